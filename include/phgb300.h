@@ -1,0 +1,211 @@
+/*
+ * phgb300.h -- C ABI of libphgb300.so, the GB300 (sm_103a) implementation of
+ * ParticleHolography.jl's reconstruction hot path.
+ *
+ * Every entry point replaces the body of one function of the reference
+ * (ParticleHolography.jl v0.2.0); the citation above each declaration names
+ * it.  A Julia wrapper keeps the reference's exported names and signatures
+ * and forwards to these symbols with `ccall`, passing `pointer(A)` of its
+ * CuArrays, the array sizes and `CUDA.stream().handle`.
+ *
+ * Conventions
+ *  - All array pointers are DEVICE pointers owned by the caller, unless the
+ *    parameter name ends in `_host`.  The library never frees caller memory.
+ *  - A Julia array of size (n_fast, n_slow) is column-major; the library
+ *    indexes the same buffer as a C-row-major [n_slow][n_fast] array.  A
+ *    volume of Julia size (n_fast, n_slow, slices) is [slices][n_slow][n_fast].
+ *  - Complex data are interleaved ComplexF32 (8 bytes: re, im).
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Every call is
+ *    asynchronous on that stream unless its comment says it synchronises.
+ *  - Every function returns PH_OK (0) or a PH_ERR_* status; ph_last_error()
+ *    gives the message.  Size errors carry the reference's @assert text.
+ *  - A ph_ctx owns scratch device memory (allocated with cudaMalloc up to the
+ *    HBM budget given at creation), twiddle tables and cached CUDA graphs.
+ *    Calls on one context are serialised: a call issued on a different stream
+ *    than the previous call first waits for the previous call's work.
+ *  - FFT lengths: every power of two from 1 to 8192 per axis (n_fast and
+ *    n_slow independently).  Other lengths return PH_ERR_UNSUPPORTED.
+ */
+#ifndef PHGB300_H
+#define PHGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define PH_API __attribute__((visibility("default")))
+#else
+#define PH_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ph_ctx ph_ctx;
+
+/* status codes */
+enum {
+    PH_OK = 0,
+    PH_ERR_SIZE = 1,        /* mirrors the size @asserts (holofunc.jl:101,185,217,249,301,341) */
+    PH_ERR_DTYPE = 2,       /* mirrors the ArgumentError of _ifft_and_abs (holofunc.jl:164) */
+    PH_ERR_TOO_LARGE = 3,   /* mirrors ccl.jl:187 (length > 2^32-1) */
+    PH_ERR_OOM = 4,         /* scratch would exceed the context's HBM budget, or cudaMalloc failed */
+    PH_ERR_CUDA = 5,        /* a CUDA runtime call or kernel launch failed */
+    PH_ERR_TIMEOUT = 6,     /* a bounded device-side loop hit its iteration limit */
+    PH_ERR_INVALID = 7,     /* null pointer, bad argument */
+    PH_ERR_UNSUPPORTED = 8  /* FFT length not supported */
+};
+
+/* element types of volumes and label inputs */
+enum {
+    PH_N0F8 = 0,   /* FixedPointNumbers.N0f8: UInt8 raw, value = raw/255 */
+    PH_F16 = 1,
+    PH_F32 = 2,
+    PH_F64 = 3,
+    PH_C64 = 4,    /* ComplexF32 */
+    PH_BOOL = 5    /* Bool / UInt8, 0 or nonzero */
+};
+
+/* options for ph_set_option */
+enum {
+    PH_OPT_SLICE_BATCH = 1,   /* slices per reconstruction batch (0 = automatic) */
+    PH_OPT_USE_GRAPHS = 2,    /* 1 = replay cached CUDA graphs for repeated shapes (default 1) */
+    PH_OPT_LOOP_LIMIT = 3     /* iteration limit of bounded device loops (CCL root chase) */
+};
+
+/* ---- context -------------------------------------------------------------- */
+
+/* Creates a context on `device`.  hbm_budget_bytes bounds the scratch memory the
+ * context may hold (0 = no bound beyond the device's free memory). */
+PH_API int32_t ph_create(int32_t device, size_t hbm_budget_bytes, ph_ctx **out);
+PH_API void ph_destroy(ph_ctx *ctx);
+PH_API const char *ph_last_error(const ph_ctx *ctx);
+PH_API int32_t ph_version(void);
+PH_API int32_t ph_set_option(ph_ctx *ctx, int32_t option, int64_t value);
+/* Bytes of scratch currently held by the context. */
+PH_API size_t ph_scratch_bytes(const ph_ctx *ctx);
+/* Pre-allocates the scratch a reconstruction of this shape needs, so that a
+ * later call allocates nothing (e.g. inside a CUDA stream capture). */
+PH_API int32_t ph_reserve(ph_ctx *ctx, int32_t n_fast, int32_t n_slow, int32_t slices, void *stream);
+/* Number of kernels this context has launched since creation. */
+PH_API int64_t ph_kernel_launches(const ph_ctx *ctx);
+
+/* ---- transfer functions ---------------------------------------------------- */
+
+/* cu_transfer_sqrt_arr (holofunc.jl:30-36; kernel holofunc.jl:8-15).
+ * out[y][x] = 1 - ((x+1 - n_fast/2 - 1)*wavlen/n_fast/dx)^2
+ *               - ((y+1 - n_slow/2 - 1)*wavlen/n_slow/dx)^2, FP64, stored Float32. */
+PH_API int32_t ph_transfer_sqrt(ph_ctx *ctx, float *out, int32_t n_fast, int32_t n_slow,
+                         double wavlen, double dx, void *stream);
+
+/* cu_transfer (holofunc.jl:61-67; kernel holofunc.jl:38-45).
+ * out = exp(i*2*pi*z0/wavlen*sqrtf(d_sqr)): Float32 sqrt, FP64 phase and
+ * sin/cos, stored ComplexF32. */
+PH_API int32_t ph_transfer(ph_ctx *ctx, void *out, const float *d_sqr, int32_t n_fast, int32_t n_slow,
+                    double z0, double wavlen, void *stream);
+
+/* No reference counterpart: the transfer function with the square-root term
+ * kept in FP64 (the exact physics) on the same centred grid as ph_transfer;
+ * evanescent frequencies are set to 0. */
+PH_API int32_t ph_transfer_fp64(ph_ctx *ctx, void *out, int32_t n_fast, int32_t n_slow,
+                         double z, double wavlen, double dx, void *stream);
+
+/* ---- wavefronts ------------------------------------------------------------- */
+
+/* cu_gabor_wavefront (holofunc.jl:80-82): out = sqrtf(holo) + 0i. */
+PH_API int32_t ph_gabor_wavefront(ph_ctx *ctx, void *out, const float *holo, int32_t n_fast, int32_t n_slow,
+                           void *stream);
+
+/* cu_2d_pad (holofunc.jl:139-149): out (2n x 2n) = mean(in), with `in` placed at
+ * rows/cols [n/2, n/2+n).  Square input only, as in the reference. */
+PH_API int32_t ph_pad2d(ph_ctx *ctx, void *out, const void *in, int32_t n_fast, int32_t n_slow, void *stream);
+
+/* cu_phase_retrieval_holo (holofunc.jl:100-129): Gerchberg-Saxton, `priter`
+ * iterations, returns the wavefront at the plane of holo1 in `out`.
+ * residual (nullable, device double): || |u2| - sqrt(I2) ||_2 / ||sqrt(I2)||_2
+ * accumulated in FP64 just before the last amplitude replacement at plane 2. */
+PH_API int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const float *holo2,
+                           const void *transfer, const void *invtransfer,
+                           int32_t n_fast, int32_t n_slow, int32_t priter,
+                           double *residual, void *stream);
+
+/* ---- propagation and reconstruction ----------------------------------------- */
+
+/* cu_asm_prop! (holofunc.jl:383-388): out = ifft(ifftshift(fftshift(fft(in)) .*
+ * cu_transfer(zprop, ..., d_sqr))).  `out` may equal `in`. */
+PH_API int32_t ph_asm_prop(ph_ctx *ctx, void *out, const void *in, const float *d_sqr, double zprop,
+                    int32_t n_fast, int32_t n_slow, double wavlen, void *stream);
+
+/* The propagation primitive shared by holofunc.jl:114,121,386:
+ * out = ifft(ifftshift(fftshift(fft(in)) .* tf)) for a caller-built centred
+ * transfer function `tf` (ComplexF32).  `out` may equal `in`. */
+PH_API int32_t ph_propagate(ph_ctx *ctx, void *out, const void *in, const void *tf, int32_t n_fast, int32_t n_slow,
+                            void *stream);
+
+/* cu_apply_low_pass_filter[!] (frequency_filters.jl:88-107):
+ * out = ifft(ifftshift(lpf .* fftshift(fft(in)))) for a centred Float32 mask.
+ * `out` may equal `in`. */
+PH_API int32_t ph_apply_lpf(ph_ctx *ctx, void *out, const void *in, const float *lpf, int32_t n_fast,
+                            int32_t n_slow, void *stream);
+
+/* cu_get_reconst_xyprojection (holofunc.jl:248-266), plus the argmin depth:
+ * proj[y][x] = min_k |ifft(ifftshift(X_k))|^2 (unclamped), X_k =
+ * fftshift(fft(wf)).*tf_front.*tf_dz^k; argmin (nullable, int32) = the first k
+ * attaining the minimum.  The volume is never stored. */
+PH_API int32_t ph_reconst_xyproj(ph_ctx *ctx, float *proj, int32_t *argmin, const void *wf,
+                          const void *tf_front, const void *tf_dz,
+                          int32_t n_fast, int32_t n_slow, int32_t slices, void *stream);
+
+/* cu_get_reconst_vol (holofunc.jl:184-200, vol_dtype N0F8/F16/F32/F64),
+ * cu_get_reconst_complex_vol (holofunc.jl:216-232, vol_dtype C64) and
+ * cu_get_reconst_vol_and_xyprojection (holofunc.jl:300-321, proj non-null:
+ * strict-< minimum over the stored, clamped and converted volume). */
+PH_API int32_t ph_reconst_vol(ph_ctx *ctx, void *vol, int32_t vol_dtype, float *proj, const void *wf,
+                       const void *tf_front, const void *tf_dz,
+                       int32_t n_fast, int32_t n_slow, int32_t slices, void *stream);
+
+/* cu_get_reconst_vol_and_xyprojection_padded (holofunc.jl:339-364): wf is
+ * n x n, the transfer functions 2n x 2n; vol is N0f8 n x n x slices (the centre
+ * crop); return_dtype is the reference's `return_type` (N0F8/F16/F32/F64). */
+PH_API int32_t ph_reconst_vol_padded(ph_ctx *ctx, uint8_t *vol, float *proj, const void *wf,
+                              const void *tf_front, const void *tf_dz,
+                              int32_t n_fast, int32_t n_slow, int32_t slices,
+                              int32_t return_dtype, void *stream);
+
+/* ---- synthetic input ----------------------------------------------------------- */
+
+/* No reference counterpart (the reference ships no generator): the seeded
+ * inline hologram of opaque discs described by its docs
+ * (whats_inline_holography.md:17-33).  discs_host is [count][4] doubles
+ * (x, y, diameter, z) in micrometres.  A unit plane wave starts at the farthest
+ * disc; at each disc plane psi *= (1 - A_i); between planes and on to z_sensor
+ * psi is propagated by the angular spectrum with FP64-phase transfer
+ * functions.  out = (|psi|^2 - min) / (max - min) + noise (noise: device
+ * Float32 array or NULL). */
+PH_API int32_t ph_synth_hologram(ph_ctx *ctx, float *out, int32_t n_fast, int32_t n_slow, const double *discs_host,
+                                 int32_t count, double wavlen, double dx, double z_sensor, const float *noise,
+                                 void *stream);
+
+/* ---- connected-component labeling -------------------------------------------- */
+
+/* cu_connected_component_labeling (ccl.jl:186-211).  `img` (F32 or BOOL) is
+ * labelled as a C-row-major rows x cols grid: 8-connected components of equal
+ * value; pixels with value > 0 get 1 + the minimum linear index of their
+ * component, others 0.  The reference's own grid is rows = size(img,1),
+ * cols = size(img,2) over the column-major buffer. */
+PH_API int32_t ph_ccl(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype,
+               int64_t rows, int64_t cols, void *stream);
+
+/* count_labels (ccl.jl:213-221) and cu_find_valid_labels (ccl.jl:224-238):
+ * writes the sorted 1-based indices i with labels[i] == i into roots_host (up to
+ * `capacity` of them, may be NULL when capacity is 0) and their number into
+ * *count_host.  Synchronises `stream`. */
+PH_API int32_t ph_ccl_roots(ph_ctx *ctx, int64_t *roots_host, int64_t capacity, int64_t *count_host,
+                     const uint32_t *labels, int64_t n, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHGB300_H */

@@ -1,0 +1,24 @@
+"""CPU oracle for the reconstruction hot path -- TEST INFRASTRUCTURE ONLY.
+
+This package restates, on the CPU, what ParticleHolography.jl computes on its
+reconstruction hot path (``src/holofunc.jl`` and ``src/ccl.jl``).  It exists so
+that the CUDA implementation can be checked against it:
+
+* ``ref_semantics`` -- the reference's own arithmetic, step by step, in
+  complex64 (Float32 square-root term, Float64 ``exp`` rounded to ComplexF32,
+  cumulative transfer products, clamp / N0f8 rounding, strict ``<`` projection).
+* ``fp64``          -- the exact angular-spectrum physics in complex128 and the
+  seeded synthetic-hologram generator used for small parity cases.
+* ``ccl``           -- the Playne-Hawick label-equivalence CCL of ``ccl.jl``
+  restated in plain C (``ccl_ref.c``), compiled with gcc and loaded by ctypes.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
+``--impl reference`` legs of ``bench.py`` may import this package, and only as
+the checker or the timed CPU baseline.  The product path never calls it.
+
+Parity status: the FFT / transfer / Gerchberg-Saxton / reconstruction rows are
+pinned only by golden vectors this oracle generates (the reference's tests hold
+no numeric values for them and its FFT is the closed cuFFT library); the CCL row
+is pinned by the reference's own known answer (84 components on
+``test/data/binaryparticles.png``).
+"""

@@ -1,0 +1,155 @@
+"""ctypes binding of libphgb300.so (the C ABI declared in include/phgb300.h).
+
+The library is built in-tree by ``build.py``.  Loading fails loudly when it is
+missing: there is no CPU path behind any entry point.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libphgb300.so"
+
+# status codes (phgb300.h)
+PH_OK = 0
+PH_ERR_SIZE = 1
+PH_ERR_DTYPE = 2
+PH_ERR_TOO_LARGE = 3
+PH_ERR_OOM = 4
+PH_ERR_CUDA = 5
+PH_ERR_TIMEOUT = 6
+PH_ERR_INVALID = 7
+PH_ERR_UNSUPPORTED = 8
+
+# element types
+PH_N0F8, PH_F16, PH_F32, PH_F64, PH_C64, PH_BOOL = range(6)
+
+# options
+PH_OPT_SLICE_BATCH = 1
+PH_OPT_USE_GRAPHS = 2
+PH_OPT_LOOP_LIMIT = 3
+
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_i64 = ctypes.c_int64
+_f64 = ctypes.c_double
+_sz = ctypes.c_size_t
+
+# name -> (restype, argtypes); every symbol include/phgb300.h declares.
+SIGNATURES = {
+    "ph_create": (_i32, [_i32, _sz, ctypes.POINTER(_vp)]),
+    "ph_destroy": (None, [_vp]),
+    "ph_last_error": (ctypes.c_char_p, [_vp]),
+    "ph_version": (_i32, []),
+    "ph_set_option": (_i32, [_vp, _i32, _i64]),
+    "ph_scratch_bytes": (_sz, [_vp]),
+    "ph_reserve": (_i32, [_vp, _i32, _i32, _i32, _vp]),
+    "ph_kernel_launches": (_i64, [_vp]),
+    "ph_transfer_sqrt": (_i32, [_vp, _vp, _i32, _i32, _f64, _f64, _vp]),
+    "ph_transfer": (_i32, [_vp, _vp, _vp, _i32, _i32, _f64, _f64, _vp]),
+    "ph_transfer_fp64": (_i32, [_vp, _vp, _i32, _i32, _f64, _f64, _f64, _vp]),
+    "ph_gabor_wavefront": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp]),
+    "ph_pad2d": (_i32, [_vp, _vp, _vp, _i32, _i32, _vp]),
+    "ph_phase_retrieval": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp]),
+    "ph_asm_prop": (_i32, [_vp, _vp, _vp, _vp, _f64, _i32, _i32, _f64, _vp]),
+    "ph_reconst_xyproj": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
+    "ph_reconst_vol": (_i32, [_vp, _vp, _i32, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
+    "ph_reconst_vol_padded": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
+    "ph_propagate": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _vp]),
+    "ph_apply_lpf": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _vp]),
+    "ph_synth_hologram": (_i32, [_vp, _vp, _i32, _i32, _vp, _i32, _f64, _f64, _f64, _vp, _vp]),
+    "ph_ccl": (_i32, [_vp, _vp, _vp, _i32, _i64, _i64, _vp]),
+    "ph_ccl_roots": (_i32, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp, _i64, _vp]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class PhError(RuntimeError):
+    """A libphgb300 call failed (CUDA error, timeout of a bounded device loop ...)."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[status {status}] {message}")
+        self.status = status
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                if not LIB_PATH.exists():
+                    raise ImportError(
+                        f"{LIB_PATH} is missing: build it with __graft_entry__.build() "
+                        "(or python particleholography.jl_gb300/build.py); there is no CPU fallback.")
+                h = ctypes.CDLL(str(LIB_PATH))
+                for name, (res, args) in SIGNATURES.items():
+                    fn = getattr(h, name)
+                    fn.restype = res
+                    fn.argtypes = args
+                _lib = h
+    return _lib
+
+
+def raise_for(status: int, ctx) -> None:
+    """Maps a status to the exception the reference raises in the same case."""
+    if status == PH_OK:
+        return
+    msg = lib().ph_last_error(ctx).decode("utf-8", "replace") if ctx else "no context"
+    if status in (PH_ERR_SIZE, PH_ERR_TOO_LARGE):
+        raise AssertionError(msg)              # the reference's @assert
+    if status == PH_ERR_DTYPE:
+        raise ValueError(msg)                  # the reference's ArgumentError
+    if status == PH_ERR_OOM:
+        raise MemoryError(msg)
+    raise PhError(status, msg)
+
+
+class Context:
+    """One ph_ctx: scratch memory, twiddle tables and cached graphs on one device."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        self.device = device
+        h = _vp()
+        st = lib().ph_create(device, hbm_budget_bytes, ctypes.byref(h))
+        if st != PH_OK:
+            raise PhError(st, f"ph_create(device={device}) failed")
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h and _lib is not None:
+            _lib.ph_destroy(h)
+            self.handle = None
+
+    def call(self, name: str, *args) -> None:
+        raise_for(getattr(lib(), name)(self.handle, *args), self.handle)
+
+    def set_option(self, option: int, value: int) -> None:
+        raise_for(lib().ph_set_option(self.handle, option, int(value)), self.handle)
+
+    @property
+    def launches(self) -> int:
+        return int(lib().ph_kernel_launches(self.handle))
+
+    @property
+    def scratch_bytes(self) -> int:
+        return int(lib().ph_scratch_bytes(self.handle))
+
+
+_contexts: dict[int, Context] = {}
+
+
+def default_context(device: int) -> Context:
+    """The process-wide context of a device (created on first use)."""
+    ctx = _contexts.get(device)
+    if ctx is None:
+        with _lock:
+            ctx = _contexts.get(device)
+            if ctx is None:
+                ctx = _contexts[device] = Context(device)
+    return ctx

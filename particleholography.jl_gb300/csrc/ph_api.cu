@@ -1,0 +1,940 @@
+// ph_api.cu -- the extern "C" entry points of libphgb300.so (declared in
+// include/phgb300.h): context management, the small setup kernels (transfer
+// functions, Gabor wavefront, padding, twiddles) and the orchestration of the
+// pass kernels for reconstruction, Gerchberg-Saxton and propagation.
+#include "phgb300.h"
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ph_ctx.h"
+#include "ph_launch.cuh"
+
+namespace ph {
+cudaError_t ccl_launch(const void *img, bool is_bool, uint32_t *lab, int64_t rows, int64_t cols, int64_t limit,
+                       int *err, cudaStream_t s, int64_t *launches);
+int64_t roots_blocks(int64_t n);
+cudaError_t roots_count_launch(const uint32_t *lab, int64_t n, unsigned *counts, unsigned long long *total,
+                               cudaStream_t s, int64_t *launches);
+cudaError_t roots_write_launch(const uint32_t *lab, int64_t n, const unsigned *offsets, long long *out,
+                               int64_t cap, cudaStream_t s, int64_t *launches);
+cudaError_t synth_fill_one(float2 *psi, size_t n, cudaStream_t s);
+cudaError_t synth_disc(float2 *psi, int nx, int ny, double cx, double cy, double diam, double dx, cudaStream_t s);
+cudaError_t synth_finish(const float2 *psi, float *out, size_t n, const float *noise, float *mm, cudaStream_t s);
+}  // namespace ph
+
+using namespace ph;
+
+namespace {
+
+constexpr int kVersion = 100;
+constexpr size_t kAlign = 256;
+constexpr int kMaxGraphs = 32;
+
+// ---------------------------------------------------------------- setup kernels
+
+__global__ void k_twiddle(float2 *tw, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s, c;
+    sincospi(-2.0 * (double)i / (double)n, &s, &c);
+    tw[i] = make_float2((float)c, (float)s);
+}
+
+// holofunc.jl:8-15 with the reference's Float64 operation order; the
+// intrinsics keep the compiler from contracting into fma.
+__device__ __forceinline__ double sqr_term(int i1, int n, double wavlen, double dx) {
+    const double a = __dsub_rn(__dsub_rn((double)i1, (double)n / 2.0), 1.0);
+    const double t = __ddiv_rn(__ddiv_rn(__dmul_rn(a, wavlen), (double)n), dx);
+    return __dmul_rn(t, t);
+}
+
+__global__ void k_transfer_sqrt(float *out, int nx, int ny, double wavlen, double dx) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= nx || y >= ny) return;
+    const double v = __dsub_rn(__dsub_rn(1.0, sqr_term(x + 1, nx, wavlen, dx)), sqr_term(y + 1, ny, wavlen, dx));
+    out[(size_t)y * nx + x] = __double2float_rn(v);
+}
+
+// holofunc.jl:38-45: exp(i * c * sqrt(Float32 d)), c = 2 pi z0 / lambda (FP64).
+__global__ void k_transfer(float2 *out, const float *d_sqr, size_t n, double c) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float s = sqrtf(d_sqr[i]);
+    const double phase = __dmul_rn(c, (double)s);
+    double sn, cs;
+    sincos(phase, &sn, &cs);
+    out[i] = make_float2(__double2float_rn(cs), __double2float_rn(sn));
+}
+
+// Exact physics: the square-root term in FP64, evanescent waves set to 0.
+__global__ void k_transfer_fp64(float2 *out, int nx, int ny, double c, double wavlen, double dx) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= nx || y >= ny) return;
+    const double s = 1.0 - sqr_term(x + 1, nx, wavlen, dx) - sqr_term(y + 1, ny, wavlen, dx);
+    float2 v = make_float2(0.f, 0.f);
+    if (s >= 0.0) {
+        double sn, cs;
+        sincos(c * sqrt(s), &sn, &cs);
+        v = make_float2((float)cs, (float)sn);
+    }
+    out[(size_t)y * nx + x] = v;
+}
+
+__global__ void k_gabor(float2 *out, const float *holo, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_float2(sqrtf(holo[i]), 0.f);
+}
+
+// Sum of a complex array in FP64 -> acc[0..1] (acc zeroed by the caller).
+__global__ void k_sum_c64(const float2 *in, size_t n, double *acc) {
+    double sx = 0.0, sy = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = in[i];
+        sx += v.x;
+        sy += v.y;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(acc, sx);
+        atomicAdd(acc + 1, sy);
+    }
+}
+
+__global__ void k_mean_finish(const double *acc, double n, float2 *mean) {
+    *mean = make_float2((float)(acc[0] / n), (float)(acc[1] / n));
+}
+
+// cu_2d_pad (holofunc.jl:139-149): out (2n)^2 filled with the mean, `in` at offset off.
+__global__ void k_pad_fill(float2 *out, const float2 *in, const float2 *mean, int nin_x, int nin_y, int nout,
+                           int off) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= nout || y >= nout) return;
+    const int xi = x - off, yi = y - off;
+    float2 v = *mean;
+    if (xi >= 0 && xi < nin_x && yi >= 0 && yi < nin_y) v = in[(size_t)yi * nin_x + xi];
+    out[(size_t)y * nout + x] = v;
+}
+
+__global__ void k_proj_finish(const unsigned long long *p64, float *proj, int32_t *argmin, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long p = p64[i];
+    if (proj) proj[i] = __uint_as_float((unsigned)(p >> 32));
+    if (argmin) argmin[i] = (int32_t)(unsigned)(p & 0xffffffffu);
+}
+
+__global__ void k_resid_finish(const double *acc, double *out) {
+    *out = acc[1] > 0.0 ? sqrt(acc[0] / acc[1]) : 0.0;
+}
+
+// ---------------------------------------------------------------- call plumbing
+
+void set_err(ph_ctx *ctx, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    ctx->err = buf;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && prev != cur) cudaSetDevice(prev);
+    }
+};
+
+int cuda_status(ph_ctx *ctx, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return PH_OK;
+    set_err(ctx, "%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? PH_ERR_OOM : PH_ERR_CUDA;
+}
+
+#define PH_TRY(expr)                                     \
+    do {                                                 \
+        int _st = (expr);                                \
+        if (_st != PH_OK) return _st;                    \
+    } while (0)
+
+#define PH_CUDA(call, what)                                  \
+    do {                                                     \
+        cudaError_t _e = (call);                             \
+        if (_e != cudaSuccess) return cuda_status(ctx, _e, what); \
+    } while (0)
+
+bool capturing(cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &st) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return st != cudaStreamCaptureStatusNone;
+}
+
+// Orders this call after the previous call of the context when it ran on a
+// different stream (the scratch arena is shared by all calls).
+int begin_call(ph_ctx *ctx, cudaStream_t s) {
+    if (ctx->has_last && ctx->last_stream != s && !capturing(s)) {
+        PH_CUDA(cudaStreamWaitEvent(s, ctx->done, 0), "cudaStreamWaitEvent");
+    }
+    return PH_OK;
+}
+
+int end_call(ph_ctx *ctx, cudaStream_t s) {
+    if (capturing(s)) return PH_OK;
+    PH_CUDA(cudaEventRecord(ctx->done, s), "cudaEventRecord");
+    ctx->last_stream = s;
+    ctx->has_last = true;
+    return PH_OK;
+}
+
+// Grows the scratch arena to at least `bytes`.  Growth waits for all earlier
+// work of the context (the old arena may still be in use) before freeing.
+int ensure_scratch(ph_ctx *ctx, size_t bytes, cudaStream_t s) {
+    if (bytes <= ctx->scratch_bytes) return PH_OK;
+    if (ctx->budget && bytes > ctx->budget) {
+        set_err(ctx, "scratch of %zu bytes exceeds the context's HBM budget of %zu bytes", bytes, ctx->budget);
+        return PH_ERR_OOM;
+    }
+    if (capturing(s)) {
+        set_err(ctx, "scratch must grow to %zu bytes during a stream capture; call ph_reserve first", bytes);
+        return PH_ERR_OOM;
+    }
+    if (ctx->scratch) {
+        PH_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        if (ctx->has_last) PH_CUDA(cudaEventSynchronize(ctx->done), "cudaEventSynchronize");
+        // Cached graphs reference the old arena.
+        for (auto &g : ctx->graphs) cudaGraphExecDestroy(g.exec);
+        ctx->graphs.clear();
+        cudaFree(ctx->scratch);
+        ctx->scratch = nullptr;
+        ctx->scratch_bytes = 0;
+    }
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_err(ctx, "cudaMalloc of %zu bytes of scratch failed: %s", bytes, cudaGetErrorString(e));
+        return PH_ERR_OOM;
+    }
+    ctx->scratch = p;
+    ctx->scratch_bytes = bytes;
+    return PH_OK;
+}
+
+struct Arena {
+    size_t off = 0;
+    template <class T>
+    size_t take(size_t count) {
+        const size_t o = (off + kAlign - 1) / kAlign * kAlign;
+        off = o + count * sizeof(T);
+        return o;
+    }
+};
+
+template <class T>
+T *at(ph_ctx *ctx, size_t off) {
+    return reinterpret_cast<T *>(static_cast<char *>(ctx->scratch) + off);
+}
+
+int get_twiddles(ph_ctx *ctx, int n, cudaStream_t s, const float2 **out) {
+    auto it = ctx->tw.find(n);
+    if (it != ctx->tw.end()) {
+        *out = it->second;
+        return PH_OK;
+    }
+    if (capturing(s)) {
+        set_err(ctx, "twiddle table for length %d must be created outside a stream capture; call ph_reserve first", n);
+        return PH_ERR_INVALID;
+    }
+    float2 *p = nullptr;
+    PH_CUDA(cudaMalloc(&p, sizeof(float2) * (size_t)n), "cudaMalloc(twiddles)");
+    k_twiddle<<<(n + 255) / 256, 256, 0, s>>>(p, n);
+    ctx->launches++;
+    PH_CUDA(cudaGetLastError(), "k_twiddle");
+    ctx->tw[n] = p;
+    *out = p;
+    return PH_OK;
+}
+
+int check_len(ph_ctx *ctx, int nx, int ny) {
+    if (nx <= 0 || ny <= 0) {
+        set_err(ctx, "array sizes must be positive. Got (%d, %d).", nx, ny);
+        return PH_ERR_SIZE;
+    }
+    if (!supported_len(nx) || !supported_len(ny)) {
+        set_err(ctx, "FFT length (%d, %d) is not supported: each axis must be a power of two up to 8192.", nx, ny);
+        return PH_ERR_UNSUPPORTED;
+    }
+    return PH_OK;
+}
+
+int launched(ph_ctx *ctx, cudaError_t e, const char *what, int count = 1) {
+    ctx->launches += count;
+    return cuda_status(ctx, e, what);
+}
+
+dim3 grid2d(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
+
+// ---------------------------------------------------------------- reconstruction plumbing
+
+struct Spectrum {
+    float4 *state;
+    const float2 *tw_x, *tw_y;
+};
+
+// Forward FFT of the (optionally mean-padded) wavefront and the spectrum state.
+// nx, ny: transform size; a1: scratch [nx][ny] complex.
+int issue_spectrum(ph_ctx *ctx, const float2 *wf, const float2 *hf, const float2 *hdz, int nx, int ny,
+                   bool padded, int nin_x, int nin_y, float2 *a1, float4 *state, const float2 *tw_x,
+                   const float2 *tw_y, double *acc, float2 *mean, cudaStream_t s) {
+    if (padded) {
+        PH_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s), "cudaMemsetAsync");
+        k_sum_c64<<<256, 256, 0, s>>>(wf, (size_t)nin_x * nin_y, acc);
+        k_mean_finish<<<1, 1, 0, s>>>(acc, (double)nin_x * nin_y, mean);
+        PH_TRY(launched(ctx, cudaGetLastError(), "mean", 2));
+        FwdRowsT<FWD_PADDED> f{};
+        f.src = wf;
+        f.dst = a1;
+        f.tw = tw_x;
+        f.pad_mean = mean;
+        f.nrows = ny;
+        f.nx_in = nin_x;
+        f.ny_in = nin_y;
+        f.pad_off = nx / 4;
+        PH_TRY(launched(ctx, launch_fwd_rows(nx, f, s), "forward rows"));
+    } else {
+        FwdRowsT<FWD_COMPLEX> f{};
+        f.src = wf;
+        f.dst = a1;
+        f.tw = tw_x;
+        f.nrows = ny;
+        PH_TRY(launched(ctx, launch_fwd_rows(nx, f, s), "forward rows"));
+    }
+    SpectrumCols c{};
+    c.a1 = a1;
+    c.hf = hf;
+    c.hdz = hdz;
+    c.state = state;
+    c.tw = tw_y;
+    c.nx = nx;
+    c.ny = ny;
+    c.scale = (float)(1.0 / ((double)nx * (double)ny));
+    PH_TRY(launched(ctx, launch_spectrum(ny, c, s), "spectrum"));
+    return PH_OK;
+}
+
+int slice_batch(ph_ctx *ctx, int nx, int ny, int slices) {
+    if (ctx->opt_slice_batch > 0) return (int)std::min<int64_t>(ctx->opt_slice_batch, slices);
+    const size_t slice_bytes = (size_t)nx * ny * sizeof(float2);
+    const size_t target = size_t(2) << 30;   // 2 GiB of slice intermediates per batch
+    int b = (int)std::max<size_t>(1, target / slice_bytes);
+    return std::min(b, slices);
+}
+
+struct ReconLayout {
+    size_t a1, state, p64, t, acc, mean, total;
+    int batch;
+};
+
+ReconLayout recon_layout(ph_ctx *ctx, int nx, int ny, int ny_out, int nx_out, int slices) {
+    ReconLayout L{};
+    L.batch = slice_batch(ctx, nx, ny, slices);
+    Arena a;
+    L.state = a.take<float4>((size_t)nx * ny);
+    L.p64 = a.take<unsigned long long>((size_t)nx_out * ny_out);
+    const size_t t_elems = std::max((size_t)L.batch * ny_out * nx, (size_t)nx * ny);   // a1 aliases t
+    L.t = a.take<float2>(t_elems);
+    L.a1 = L.t;
+    L.acc = a.take<double>(4);
+    L.mean = a.take<float2>(1);
+    L.total = a.off;
+    return L;
+}
+
+enum ReconKind { RK_PROJ, RK_VOL, RK_CVOL, RK_PADDED };
+
+// Shared driver of every reconstruction entry point.
+int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype,
+                const float2 *wf, const float2 *hf, const float2 *hdz, int nin_x, int nin_y, int slices,
+                cudaStream_t s) {
+    const bool padded = kind == RK_PADDED;
+    const int nx = padded ? 2 * nin_x : nin_x;
+    const int ny = padded ? 2 * nin_y : nin_y;
+    PH_TRY(check_len(ctx, nx, ny));
+    const int nx_out = nin_x, ny_out = nin_y;
+    const int x0 = padded ? nin_x / 2 : 0;
+    const int y0 = padded ? nin_y / 2 : 0;
+    ReconLayout L = recon_layout(ctx, nx, ny, ny_out, nx_out, slices);
+    PH_TRY(ensure_scratch(ctx, L.total, s));
+    const float2 *tw_x = nullptr, *tw_y = nullptr;
+    PH_TRY(get_twiddles(ctx, nx, s, &tw_x));
+    PH_TRY(get_twiddles(ctx, ny, s, &tw_y));
+    float4 *state = at<float4>(ctx, L.state);
+    auto *p64 = at<unsigned long long>(ctx, L.p64);
+    float2 *t = at<float2>(ctx, L.t);
+    PH_TRY(issue_spectrum(ctx, wf, hf, hdz, nx, ny, padded, nin_x, nin_y, at<float2>(ctx, L.a1), state, tw_x,
+                          tw_y, at<double>(ctx, L.acc), at<float2>(ctx, L.mean), s));
+    const bool want_proj = (kind == RK_PROJ) || proj != nullptr || argmin != nullptr;
+    if (want_proj) PH_CUDA(cudaMemsetAsync(p64, 0xff, sizeof(unsigned long long) * nx_out * ny_out, s), "memset");
+
+    const int group = 8;
+    for (int k0 = 0; k0 < slices; k0 += L.batch) {
+        const int nb = std::min(L.batch, slices - k0);
+        ReconA a{};
+        a.state = state;
+        a.t = t;
+        a.tw = tw_y;
+        a.nx = nx;
+        a.ny_out = ny_out;
+        a.y0 = y0;
+        a.k0 = k0;
+        PH_TRY(launched(ctx, launch_recon_a(ny, a, nb, s), "reconstruction pass A"));
+        if (kind == RK_PROJ) {
+            ReconB<EPI_PROJ> b{};
+            b.t = t; b.tw = tw_x; b.proj64 = p64; b.rows = ny_out; b.nx_out = nx_out; b.x0 = 0;
+            b.k0 = k0; b.nbatch = nb; b.group = group; b.vol_slice_stride = (long long)nx_out * ny_out;
+            PH_TRY(launched(ctx, launch_recon_b(nx, b, s), "reconstruction pass B"));
+        } else if (kind == RK_CVOL) {
+            ReconB<EPI_CVOL> b{};
+            b.t = t; b.tw = tw_x; b.vol = vol; b.rows = ny_out; b.nx_out = nx_out; b.x0 = 0;
+            b.k0 = k0; b.nbatch = nb; b.group = 1; b.vol_slice_stride = (long long)nx_out * ny_out;
+            PH_TRY(launched(ctx, launch_recon_b(nx, b, s), "reconstruction pass B"));
+        } else {
+            ReconB<EPI_VOL> b{};
+            b.t = t; b.tw = tw_x; b.vol = vol; b.vol_dtype = vol_dtype; b.proj64 = want_proj ? p64 : nullptr;
+            b.rows = ny_out; b.nx_out = nx_out; b.x0 = x0;
+            b.k0 = k0; b.nbatch = nb; b.group = group; b.vol_slice_stride = (long long)nx_out * ny_out;
+            PH_TRY(launched(ctx, launch_recon_b(nx, b, s), "reconstruction pass B"));
+        }
+    }
+    if (want_proj) {
+        const size_t n = (size_t)nx_out * ny_out;
+        k_proj_finish<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p64, proj, argmin, n);
+        PH_TRY(launched(ctx, cudaGetLastError(), "projection finish"));
+    }
+    return PH_OK;
+}
+
+// ---------------------------------------------------------------- propagation plumbing
+
+// out = IFFT2( FFT2(in) .* H(centred) ) with H = transfer (or real mask).
+int issue_propagate(ph_ctx *ctx, float2 *out, const float2 *in, const float2 *h, const float *mask, int nx, int ny,
+                    float2 *bufa, float2 *bufb, const float2 *tw_x, const float2 *tw_y, cudaStream_t s) {
+    FwdRowsT<FWD_COMPLEX> f{};
+    f.src = in;
+    f.dst = bufa;
+    f.tw = tw_x;
+    f.nrows = ny;
+    PH_TRY(launched(ctx, launch_fwd_rows(nx, f, s), "forward rows"));
+    GsCol c{};
+    c.src = bufa;
+    c.h = h;
+    c.mask = mask;
+    c.dst = bufb;
+    c.tw = tw_y;
+    c.nx = nx;
+    c.scale = (float)(1.0 / ((double)nx * (double)ny));
+    PH_TRY(launched(ctx, launch_gs_col(ny, c, s), "column pass"));
+    GsRow<ROW_INV> r{};
+    r.src = bufb;
+    r.dst = out;
+    r.tw = tw_x;
+    r.nrows = ny;
+    PH_TRY(launched(ctx, launch_gs_row(nx, r, s), "inverse rows"));
+    return PH_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+
+#define PH_ENTER(ctx, stream)                             \
+    if ((ctx) == nullptr) return PH_ERR_INVALID;          \
+    std::lock_guard<std::mutex> _lk((ctx)->mu);           \
+    DeviceGuard _dg((ctx)->device);                       \
+    cudaStream_t s = static_cast<cudaStream_t>(stream);   \
+    PH_TRY(begin_call((ctx), s))
+
+#define PH_LEAVE(ctx) return end_call((ctx), s)
+
+#define PH_NONNULL(p, name)                                           \
+    do {                                                              \
+        if ((p) == nullptr) {                                         \
+            set_err(ctx, "%s must not be NULL", name);                \
+            return PH_ERR_INVALID;                                    \
+        }                                                             \
+    } while (0)
+
+extern "C" {
+
+int32_t ph_version(void) { return kVersion; }
+
+int32_t ph_create(int32_t device, size_t hbm_budget_bytes, ph_ctx **out) {
+    if (out == nullptr) return PH_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return PH_ERR_CUDA;
+    }
+    ph_ctx *ctx = new ph_ctx();
+    ctx->device = device;
+    ctx->budget = hbm_budget_bytes;
+    DeviceGuard g(device);
+    if (cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&ctx->small, 256) != cudaSuccess || cudaMemset(ctx->small, 0, 256) != cudaSuccess) {
+        cudaGetLastError();
+        ph_destroy(ctx);
+        return PH_ERR_CUDA;
+    }
+    *out = ctx;
+    return PH_OK;
+}
+
+void ph_destroy(ph_ctx *ctx) {
+    if (ctx == nullptr) return;
+    {
+        DeviceGuard g(ctx->device);
+        cudaDeviceSynchronize();
+        for (auto &gr : ctx->graphs) cudaGraphExecDestroy(gr.exec);
+        for (auto &kv : ctx->tw) cudaFree(kv.second);
+        if (ctx->scratch) cudaFree(ctx->scratch);
+        if (ctx->small) cudaFree(ctx->small);
+        if (ctx->done) cudaEventDestroy(ctx->done);
+        if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
+        cudaGetLastError();
+    }
+    delete ctx;
+}
+
+const char *ph_last_error(const ph_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int32_t ph_set_option(ph_ctx *ctx, int32_t option, int64_t value) {
+    if (ctx == nullptr) return PH_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    switch (option) {
+        case PH_OPT_SLICE_BATCH: ctx->opt_slice_batch = value; return PH_OK;
+        case PH_OPT_USE_GRAPHS: ctx->opt_use_graphs = value; return PH_OK;
+        case PH_OPT_LOOP_LIMIT:
+            if (value < 1) return PH_ERR_INVALID;
+            ctx->opt_loop_limit = value;
+            return PH_OK;
+    }
+    set_err(ctx, "unknown option %d", option);
+    return PH_ERR_INVALID;
+}
+
+size_t ph_scratch_bytes(const ph_ctx *ctx) { return ctx ? ctx->scratch_bytes : 0; }
+int64_t ph_kernel_launches(const ph_ctx *ctx) { return ctx ? ctx->launches.load() : 0; }
+
+int32_t ph_reserve(ph_ctx *ctx, int32_t n_fast, int32_t n_slow, int32_t slices, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_TRY(check_len(ctx, n_fast, n_slow));
+    ReconLayout L = recon_layout(ctx, n_fast, n_slow, n_slow, n_fast, std::max(1, (int)slices));
+    const size_t gs = 2 * sizeof(float2) * (size_t)n_fast * n_slow + 2 * kAlign;
+    PH_TRY(ensure_scratch(ctx, std::max(L.total, gs), s));
+    const float2 *tw = nullptr;
+    PH_TRY(get_twiddles(ctx, n_fast, s, &tw));
+    PH_TRY(get_twiddles(ctx, n_slow, s, &tw));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_transfer_sqrt(ph_ctx *ctx, float *out, int32_t n_fast, int32_t n_slow, double wavlen, double dx,
+                         void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    if (n_fast <= 0 || n_slow <= 0) { set_err(ctx, "sizes must be positive"); return PH_ERR_SIZE; }
+    dim3 b(32, 8);
+    k_transfer_sqrt<<<grid2d(n_fast, n_slow, b), b, 0, s>>>(out, n_fast, n_slow, wavlen, dx);
+    PH_TRY(launched(ctx, cudaGetLastError(), "transfer_sqrt"));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_transfer(ph_ctx *ctx, void *out, const float *d_sqr, int32_t n_fast, int32_t n_slow, double z0,
+                    double wavlen, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(d_sqr, "d_sqr");
+    if (n_fast <= 0 || n_slow <= 0) { set_err(ctx, "sizes must be positive"); return PH_ERR_SIZE; }
+    const size_t n = (size_t)n_fast * n_slow;
+    const double c = (2.0 * M_PI * z0) / wavlen;
+    k_transfer<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<float2 *>(out), d_sqr, n, c);
+    PH_TRY(launched(ctx, cudaGetLastError(), "transfer"));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_transfer_fp64(ph_ctx *ctx, void *out, int32_t n_fast, int32_t n_slow, double z, double wavlen, double dx,
+                         void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    if (n_fast <= 0 || n_slow <= 0) { set_err(ctx, "sizes must be positive"); return PH_ERR_SIZE; }
+    dim3 b(32, 8);
+    const double c = (2.0 * M_PI * z) / wavlen;
+    k_transfer_fp64<<<grid2d(n_fast, n_slow, b), b, 0, s>>>(static_cast<float2 *>(out), n_fast, n_slow, c, wavlen,
+                                                          dx);
+    PH_TRY(launched(ctx, cudaGetLastError(), "transfer_fp64"));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_gabor_wavefront(ph_ctx *ctx, void *out, const float *holo, int32_t n_fast, int32_t n_slow,
+                           void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(holo, "holo");
+    if (n_fast <= 0 || n_slow <= 0) { set_err(ctx, "sizes must be positive"); return PH_ERR_SIZE; }
+    const size_t n = (size_t)n_fast * n_slow;
+    k_gabor<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(static_cast<float2 *>(out), holo, n);
+    PH_TRY(launched(ctx, cudaGetLastError(), "gabor"));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_pad2d(ph_ctx *ctx, void *out, const void *in, int32_t n_fast, int32_t n_slow, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(in, "in");
+    if (n_fast <= 0 || n_slow <= 0 || n_fast != n_slow) {
+        set_err(ctx, "cu_2d_pad needs a square input. Got (%d, %d).", n_fast, n_slow);
+        return PH_ERR_SIZE;
+    }
+    PH_TRY(ensure_scratch(ctx, 2 * kAlign, s));
+    double *acc = at<double>(ctx, 0);
+    float2 *mean = at<float2>(ctx, kAlign);
+    PH_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s), "cudaMemsetAsync");
+    const size_t n = (size_t)n_fast * n_slow;
+    k_sum_c64<<<256, 256, 0, s>>>(static_cast<const float2 *>(in), n, acc);
+    k_mean_finish<<<1, 1, 0, s>>>(acc, (double)n, mean);
+    const int nout = 2 * n_fast;
+    dim3 b(32, 8);
+    k_pad_fill<<<grid2d(nout, nout, b), b, 0, s>>>(static_cast<float2 *>(out), static_cast<const float2 *>(in), mean,
+                                                  n_fast, n_slow, nout, nout / 4);
+    PH_TRY(launched(ctx, cudaGetLastError(), "pad2d", 3));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const float *holo2, const void *transfer,
+                           const void *invtransfer, int32_t n_fast, int32_t n_slow, int32_t priter, double *residual,
+                           void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(holo1, "holo1");
+    PH_NONNULL(holo2, "holo2");
+    PH_NONNULL(transfer, "transfer");
+    PH_NONNULL(invtransfer, "invtransfer");
+    PH_TRY(check_len(ctx, n_fast, n_slow));
+    if (priter < 0) { set_err(ctx, "priter must be >= 0"); return PH_ERR_INVALID; }
+    const int nx = n_fast, ny = n_slow;
+    const size_t n = (size_t)nx * ny;
+    float2 *o = static_cast<float2 *>(out);
+    double *acc = reinterpret_cast<double *>(static_cast<char *>(ctx->small) + 64);
+    if (priter == 0) {   // light1 = sqrt(I1) + 0im
+        k_gabor<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(o, holo1, n);
+        PH_TRY(launched(ctx, cudaGetLastError(), "gabor"));
+        if (residual) PH_CUDA(cudaMemsetAsync(residual, 0, sizeof(double), s), "memset");
+        PH_LEAVE(ctx);
+    }
+    Arena a;
+    const size_t oa = a.take<float2>(n), ob = a.take<float2>(n);
+    PH_TRY(ensure_scratch(ctx, a.off, s));
+    float2 *bufa = at<float2>(ctx, oa), *bufb = at<float2>(ctx, ob);
+    const float2 *tw_x = nullptr, *tw_y = nullptr;
+    PH_TRY(get_twiddles(ctx, nx, s, &tw_x));
+    PH_TRY(get_twiddles(ctx, ny, s, &tw_y));
+    if (residual) PH_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s), "memset");
+
+    FwdRowsT<FWD_SQRT_REAL> f{};
+    f.src_real = holo1;
+    f.dst = bufa;
+    f.tw = tw_x;
+    f.nrows = ny;
+    PH_TRY(launched(ctx, launch_fwd_rows(nx, f, s), "GS first rows"));
+    const float scale = (float)(1.0 / ((double)nx * (double)ny));
+    for (int it = 0; it < priter; ++it) {
+        const bool last = it == priter - 1;
+        GsCol c{};
+        c.src = bufa; c.h = static_cast<const float2 *>(transfer); c.dst = bufb; c.tw = tw_y; c.nx = nx;
+        c.scale = scale;
+        PH_TRY(launched(ctx, launch_gs_col(ny, c, s), "GS column pass"));
+        GsRow<ROW_MID> r2{};
+        r2.src = bufb; r2.holo = holo2; r2.dst = bufa; r2.tw = tw_x; r2.nrows = ny;
+        r2.resid = (last && residual) ? acc : nullptr;
+        PH_TRY(launched(ctx, launch_gs_row(nx, r2, s), "GS row pass (plane 2)"));
+        c.src = bufa; c.h = static_cast<const float2 *>(invtransfer); c.dst = bufb;
+        PH_TRY(launched(ctx, launch_gs_col(ny, c, s), "GS column pass"));
+        if (!last) {
+            GsRow<ROW_MID> r1{};
+            r1.src = bufb; r1.holo = holo1; r1.dst = bufa; r1.tw = tw_x; r1.nrows = ny;
+            PH_TRY(launched(ctx, launch_gs_row(nx, r1, s), "GS row pass (plane 1)"));
+        } else {
+            GsRow<ROW_FINAL> r1{};
+            r1.src = bufb; r1.holo = holo1; r1.dst = o; r1.tw = tw_x; r1.nrows = ny;
+            PH_TRY(launched(ctx, launch_gs_row(nx, r1, s), "GS final row pass"));
+        }
+    }
+    if (residual) {
+        k_resid_finish<<<1, 1, 0, s>>>(acc, residual);
+        PH_TRY(launched(ctx, cudaGetLastError(), "GS residual"));
+    }
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_asm_prop(ph_ctx *ctx, void *out, const void *in, const float *d_sqr, double zprop, int32_t n_fast,
+                    int32_t n_slow, double wavlen, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(in, "in");
+    PH_NONNULL(d_sqr, "d_sqr");
+    PH_TRY(check_len(ctx, n_fast, n_slow));
+    const int nx = n_fast, ny = n_slow;
+    const size_t n = (size_t)nx * ny;
+    Arena a;
+    const size_t oh = a.take<float2>(n), oa = a.take<float2>(n), ob = a.take<float2>(n);
+    PH_TRY(ensure_scratch(ctx, a.off, s));
+    const float2 *tw_x = nullptr, *tw_y = nullptr;
+    PH_TRY(get_twiddles(ctx, nx, s, &tw_x));
+    PH_TRY(get_twiddles(ctx, ny, s, &tw_y));
+    float2 *h = at<float2>(ctx, oh);
+    const double c = (2.0 * M_PI * zprop) / wavlen;
+    k_transfer<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(h, d_sqr, n, c);
+    PH_TRY(launched(ctx, cudaGetLastError(), "transfer"));
+    PH_TRY(issue_propagate(ctx, static_cast<float2 *>(out), static_cast<const float2 *>(in), h, nullptr, nx, ny,
+                           at<float2>(ctx, oa), at<float2>(ctx, ob), tw_x, tw_y, s));
+    PH_LEAVE(ctx);
+}
+
+static int propagate_common(ph_ctx *ctx, void *out, const void *in, const float2 *tf, const float *mask, int nx,
+                            int ny, cudaStream_t s) {
+    PH_TRY(check_len(ctx, nx, ny));
+    const size_t n = (size_t)nx * ny;
+    Arena a;
+    const size_t oa = a.take<float2>(n), ob = a.take<float2>(n);
+    PH_TRY(ensure_scratch(ctx, a.off, s));
+    const float2 *tw_x = nullptr, *tw_y = nullptr;
+    PH_TRY(get_twiddles(ctx, nx, s, &tw_x));
+    PH_TRY(get_twiddles(ctx, ny, s, &tw_y));
+    return issue_propagate(ctx, static_cast<float2 *>(out), static_cast<const float2 *>(in), tf, mask, nx, ny,
+                           at<float2>(ctx, oa), at<float2>(ctx, ob), tw_x, tw_y, s);
+}
+
+int32_t ph_propagate(ph_ctx *ctx, void *out, const void *in, const void *tf, int32_t n_fast, int32_t n_slow,
+                     void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(in, "in");
+    PH_NONNULL(tf, "tf");
+    PH_TRY(propagate_common(ctx, out, in, static_cast<const float2 *>(tf), nullptr, n_fast, n_slow, s));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_apply_lpf(ph_ctx *ctx, void *out, const void *in, const float *lpf, int32_t n_fast, int32_t n_slow,
+                     void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(in, "in");
+    PH_NONNULL(lpf, "lpf");
+    PH_TRY(propagate_common(ctx, out, in, nullptr, lpf, n_fast, n_slow, s));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_synth_hologram(ph_ctx *ctx, float *out, int32_t n_fast, int32_t n_slow, const double *discs_host,
+                          int32_t count, double wavlen, double dx, double z_sensor, const float *noise,
+                          void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    if (count > 0) PH_NONNULL(discs_host, "discs");
+    if (count < 0) { set_err(ctx, "negative disc count"); return PH_ERR_INVALID; }
+    PH_TRY(check_len(ctx, n_fast, n_slow));
+    const int nx = n_fast, ny = n_slow;
+    const size_t n = (size_t)nx * ny;
+    Arena a;
+    const size_t opsi = a.take<float2>(n), oh = a.take<float2>(n), oa = a.take<float2>(n), ob = a.take<float2>(n);
+    const size_t omm = a.take<float>(2);
+    PH_TRY(ensure_scratch(ctx, a.off, s));
+    const float2 *tw_x = nullptr, *tw_y = nullptr;
+    PH_TRY(get_twiddles(ctx, nx, s, &tw_x));
+    PH_TRY(get_twiddles(ctx, ny, s, &tw_y));
+    float2 *psi = at<float2>(ctx, opsi), *h = at<float2>(ctx, oh);
+    // farthest disc first (stable on ties)
+    std::vector<int> order(count);
+    for (int i = 0; i < count; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int p, int q) { return discs_host[4 * p + 3] > discs_host[4 * q + 3]; });
+    PH_TRY(launched(ctx, synth_fill_one(psi, n, s), "synth fill"));
+    dim3 b(32, 8);
+    auto propagate_by = [&](double z) -> int {
+        const double c = (2.0 * M_PI * z) / wavlen;
+        k_transfer_fp64<<<grid2d(nx, ny, b), b, 0, s>>>(h, nx, ny, c, wavlen, dx);
+        PH_TRY(launched(ctx, cudaGetLastError(), "synth transfer"));
+        return issue_propagate(ctx, psi, psi, h, nullptr, nx, ny, at<float2>(ctx, oa), at<float2>(ctx, ob), tw_x,
+                               tw_y, s);
+    };
+    double zc = count > 0 ? discs_host[4 * order[0] + 3] : z_sensor;
+    for (int k = 0; k < count; ++k) {
+        const double *d = discs_host + 4 * order[k];
+        if (d[3] != zc) {
+            PH_TRY(propagate_by(zc - d[3]));
+            zc = d[3];
+        }
+        PH_TRY(launched(ctx, synth_disc(psi, nx, ny, d[0], d[1], d[2], dx, s), "synth disc"));
+    }
+    PH_TRY(propagate_by(zc - z_sensor));
+    PH_TRY(launched(ctx, synth_finish(psi, out, n, noise, at<float>(ctx, omm), s), "synth finish", 3));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_reconst_xyproj(ph_ctx *ctx, float *proj, int32_t *argmin, const void *wf, const void *tf_front,
+                          const void *tf_dz, int32_t n_fast, int32_t n_slow, int32_t slices, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(wf, "wavefront");
+    PH_NONNULL(tf_front, "transfer_front");
+    PH_NONNULL(tf_dz, "transfer_dz");
+    if (proj == nullptr && argmin == nullptr) { set_err(ctx, "proj and argmin are both NULL"); return PH_ERR_INVALID; }
+    if (slices < 1) { set_err(ctx, "slices must be >= 1. Got %d.", slices); return PH_ERR_SIZE; }
+    PH_TRY(reconstruct(ctx, RK_PROJ, proj, argmin, nullptr, PH_F32, static_cast<const float2 *>(wf),
+                       static_cast<const float2 *>(tf_front), static_cast<const float2 *>(tf_dz), n_fast, n_slow,
+                       slices, s));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_reconst_vol(ph_ctx *ctx, void *vol, int32_t vol_dtype, float *proj, const void *wf, const void *tf_front,
+                       const void *tf_dz, int32_t n_fast, int32_t n_slow, int32_t slices, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(vol, "vol");
+    PH_NONNULL(wf, "wavefront");
+    PH_NONNULL(tf_front, "transfer_front");
+    PH_NONNULL(tf_dz, "transfer_dz");
+    if (slices < 1) { set_err(ctx, "slices must be >= 1. Got %d.", slices); return PH_ERR_SIZE; }
+    if (vol_dtype < PH_N0F8 || vol_dtype > PH_C64) {
+        set_err(ctx, "return_type must be Subtype of AbstractFloat or N0f8. Got dtype code %d", vol_dtype);
+        return PH_ERR_DTYPE;
+    }
+    if (vol_dtype == PH_C64 && proj != nullptr) {
+        set_err(ctx, "a complex volume has no xy projection");
+        return PH_ERR_INVALID;
+    }
+    PH_TRY(reconstruct(ctx, vol_dtype == PH_C64 ? RK_CVOL : RK_VOL, proj, nullptr, vol, vol_dtype,
+                       static_cast<const float2 *>(wf), static_cast<const float2 *>(tf_front),
+                       static_cast<const float2 *>(tf_dz), n_fast, n_slow, slices, s));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_reconst_vol_padded(ph_ctx *ctx, uint8_t *vol, float *proj, const void *wf, const void *tf_front,
+                              const void *tf_dz, int32_t n_fast, int32_t n_slow, int32_t slices, int32_t return_dtype,
+                              void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(vol, "vol");
+    PH_NONNULL(wf, "wavefront");
+    PH_NONNULL(tf_front, "transfer_front");
+    PH_NONNULL(tf_dz, "transfer_dz");
+    if (slices < 1) { set_err(ctx, "slices must be >= 1. Got %d.", slices); return PH_ERR_SIZE; }
+    if (return_dtype < PH_N0F8 || return_dtype > PH_F64) {
+        set_err(ctx, "return_type must be Subtype of AbstractFloat or N0f8. Got dtype code %d", return_dtype);
+        return PH_ERR_DTYPE;
+    }
+    if (n_fast != n_slow || (n_fast & 1)) {
+        set_err(ctx, "the padded reconstruction needs a square input of even size. Got (%d, %d).", n_fast, n_slow);
+        return PH_ERR_SIZE;
+    }
+    PH_TRY(reconstruct(ctx, RK_PADDED, proj, nullptr, vol, PH_N0F8, static_cast<const float2 *>(wf),
+                       static_cast<const float2 *>(tf_front), static_cast<const float2 *>(tf_dz), n_fast, n_slow,
+                       slices, s));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_ccl(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype, int64_t rows, int64_t cols,
+               void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(labels, "labels");
+    PH_NONNULL(img, "img");
+    if (rows < 0 || cols < 0) { set_err(ctx, "negative size"); return PH_ERR_SIZE; }
+    if ((unsigned long long)rows * (unsigned long long)cols > 4294967295ull) {
+        set_err(ctx, "Image is too large. Maximum length is 2^32-1.");
+        return PH_ERR_TOO_LARGE;
+    }
+    if (img_dtype != PH_F32 && img_dtype != PH_BOOL) {
+        set_err(ctx, "labeling input must be Float32 or Bool. Got dtype code %d", img_dtype);
+        return PH_ERR_DTYPE;
+    }
+    int64_t nl = 0;
+    cudaError_t e = ccl_launch(img, img_dtype == PH_BOOL, labels, rows, cols, ctx->opt_loop_limit,
+                               static_cast<int *>(ctx->small), s, &nl);
+    ctx->launches += nl;
+    PH_TRY(cuda_status(ctx, e, "labeling"));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_ccl_roots(ph_ctx *ctx, int64_t *roots_host, int64_t capacity, int64_t *count_host, const uint32_t *labels,
+                     int64_t n, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(labels, "labels");
+    PH_NONNULL(count_host, "count");
+    if (capacity > 0) PH_NONNULL(roots_host, "roots");
+    if (n < 0) { set_err(ctx, "negative size"); return PH_ERR_SIZE; }
+    *count_host = 0;
+    if (n == 0) PH_LEAVE(ctx);
+    const int64_t nb = roots_blocks(n);
+    Arena a;
+    const size_t oc = a.take<unsigned>(nb);
+    const size_t ot = a.take<unsigned long long>(1);
+    PH_TRY(ensure_scratch(ctx, a.off, s));
+    int64_t nl = 0;
+    PH_TRY(cuda_status(ctx, roots_count_launch(labels, n, at<unsigned>(ctx, oc), at<unsigned long long>(ctx, ot), s,
+                                               &nl), "root count"));
+    unsigned long long total = 0;
+    int flag = 0;
+    PH_CUDA(cudaMemcpyAsync(&total, at<unsigned long long>(ctx, ot), sizeof total, cudaMemcpyDeviceToHost, s),
+            "copy count");
+    PH_CUDA(cudaMemcpyAsync(&flag, ctx->small, sizeof flag, cudaMemcpyDeviceToHost, s), "copy flag");
+    PH_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (flag) {
+        cudaMemsetAsync(ctx->small, 0, sizeof(int), s);
+        set_err(ctx, "a labeling loop reached its iteration limit; labels are incomplete");
+        ctx->launches += nl;
+        return PH_ERR_TIMEOUT;
+    }
+    *count_host = (int64_t)total;
+    const int64_t want = std::min<int64_t>((int64_t)total, capacity);
+    if (want > 0) {
+        Arena b = a;
+        const size_t orr = b.take<long long>((size_t)want);
+        // the offsets and total live below `orr`; growing would discard them, so size first
+        if (b.off > ctx->scratch_bytes) {
+            PH_TRY(ensure_scratch(ctx, b.off, s));
+            PH_TRY(cuda_status(ctx, roots_count_launch(labels, n, at<unsigned>(ctx, oc),
+                                                       at<unsigned long long>(ctx, ot), s, &nl), "root count"));
+        }
+        PH_TRY(cuda_status(ctx, roots_write_launch(labels, n, at<unsigned>(ctx, oc), at<long long>(ctx, orr), want, s,
+                                                   &nl), "root write"));
+        PH_CUDA(cudaMemcpyAsync(roots_host, at<long long>(ctx, orr), sizeof(long long) * want, cudaMemcpyDeviceToHost,
+                                s), "copy roots");
+        PH_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    }
+    ctx->launches += nl;
+    PH_LEAVE(ctx);
+}
+
+}  // extern "C"

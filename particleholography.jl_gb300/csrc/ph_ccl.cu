@@ -1,0 +1,233 @@
+// ph_ccl.cu -- connected-component labeling of equal-valued 8-connected
+// regions (the semantics of ParticleHolography.jl src/ccl.jl:186-211) by
+// lock-free union-find, plus the root compaction behind count_labels /
+// cu_find_valid_labels (ccl.jl:213-238).
+//
+// Every label array satisfies L[i] <= i; a union links the larger of two roots
+// to the smaller with atomicMin, so every tree's root is the minimum linear
+// index of its component and the final label (root + 1) matches the
+// reference's.  Chains strictly decrease, so every chase ends; each loop still
+// carries an iteration limit that raises the context's error flag.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ph {
+
+constexpr int kCclBlockX = 32;
+constexpr int kCclBlockY = 8;
+
+template <class T>
+__device__ __forceinline__ bool ccl_fg(T v);
+template <>
+__device__ __forceinline__ bool ccl_fg<float>(float v) { return v > 0.0f; }
+template <>
+__device__ __forceinline__ bool ccl_fg<uint8_t>(uint8_t v) { return v != 0; }
+
+// Equality of pixel values: Float32 compares the values, Bool its truth.
+__device__ __forceinline__ bool ccl_eq(float a, float b) { return a == b; }
+__device__ __forceinline__ bool ccl_eq(uint8_t a, uint8_t b) { return (a != 0) == (b != 0); }
+
+__device__ __forceinline__ uint32_t ccl_find(const uint32_t *__restrict__ lab, uint32_t x, int64_t limit,
+                                             int *err) {
+    uint32_t p = lab[x];
+    int64_t it = 0;
+    while (p != x) {
+        x = p;
+        p = lab[x];
+        if (++it > limit) { atomicExch(err, 1); break; }
+    }
+    return x;
+}
+
+// Volatile-free find for the union phase: labels change under us, so re-read.
+__device__ __forceinline__ uint32_t ccl_find_live(uint32_t *lab, uint32_t x, int64_t limit, int *err) {
+    uint32_t p = __ldcg(lab + x);
+    int64_t it = 0;
+    while (p != x) {
+        x = p;
+        p = __ldcg(lab + x);
+        if (++it > limit) { atomicExch(err, 1); break; }
+    }
+    return x;
+}
+
+__device__ __forceinline__ void ccl_unite(uint32_t *lab, uint32_t a, uint32_t b, int64_t limit, int *err) {
+    int64_t it = 0;
+    while (true) {
+        a = ccl_find_live(lab, a, limit, err);
+        b = ccl_find_live(lab, b, limit, err);
+        if (a == b) return;
+        if (a < b) { uint32_t t = a; a = b; b = t; }
+        const uint32_t old = atomicMin(lab + a, b);
+        if (old == a) return;
+        a = old;
+        if (++it > limit) { atomicExch(err, 1); return; }
+    }
+}
+
+__global__ void k_ccl_init(uint32_t *lab, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) lab[i] = (uint32_t)i;
+}
+
+template <class T>
+__global__ void k_ccl_union(const T *__restrict__ img, uint32_t *lab, int64_t rows, int64_t cols, int64_t limit,
+                            int *err) {
+    const int64_t x = (int64_t)blockIdx.x * kCclBlockX + threadIdx.x;
+    const int64_t y = (int64_t)blockIdx.y * kCclBlockY + threadIdx.y;
+    if (x >= cols || y >= rows) return;
+    const int64_t i = y * cols + x;
+    const T v = img[i];
+    if (!ccl_fg<T>(v)) return;
+    if (x > 0 && ccl_eq(img[i - 1], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)(i - 1), limit, err);
+    if (y > 0) {
+        const int64_t u = i - cols;
+        if (x > 0 && ccl_eq(img[u - 1], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)(u - 1), limit, err);
+        if (ccl_eq(img[u], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)u, limit, err);
+        if (x + 1 < cols && ccl_eq(img[u + 1], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)(u + 1), limit, err);
+    }
+}
+
+template <class T>
+__global__ void k_ccl_compress(const T *__restrict__ img, uint32_t *lab, int64_t n, int64_t limit, int *err) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (ccl_fg<T>(img[i])) lab[i] = ccl_find_live(lab, (uint32_t)i, limit, err);
+}
+
+template <class T>
+__global__ void k_ccl_background(const T *__restrict__ img, uint32_t *lab, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    lab[i] = ccl_fg<T>(img[i]) ? lab[i] + 1u : 0u;
+}
+
+template <class T>
+static cudaError_t ccl_run(const T *img, uint32_t *lab, int64_t rows, int64_t cols, int64_t limit, int *err,
+                           cudaStream_t s, int64_t *launches) {
+    const int64_t n = rows * cols;
+    const int tpb = 256;
+    const unsigned g1 = (unsigned)((n + tpb - 1) / tpb);
+    k_ccl_init<<<g1, tpb, 0, s>>>(lab, n);
+    dim3 b2(kCclBlockX, kCclBlockY);
+    dim3 g2((unsigned)((cols + kCclBlockX - 1) / kCclBlockX), (unsigned)((rows + kCclBlockY - 1) / kCclBlockY));
+    k_ccl_union<T><<<g2, b2, 0, s>>>(img, lab, rows, cols, limit, err);
+    k_ccl_compress<T><<<g1, tpb, 0, s>>>(img, lab, n, limit, err);
+    k_ccl_background<T><<<g1, tpb, 0, s>>>(img, lab, n);
+    *launches += 4;
+    return cudaGetLastError();
+}
+
+cudaError_t ccl_launch(const void *img, bool is_bool, uint32_t *lab, int64_t rows, int64_t cols, int64_t limit,
+                       int *err, cudaStream_t s, int64_t *launches) {
+    if (rows <= 0 || cols <= 0) return cudaSuccess;
+    if (is_bool) return ccl_run<uint8_t>(static_cast<const uint8_t *>(img), lab, rows, cols, limit, err, s, launches);
+    return ccl_run<float>(static_cast<const float *>(img), lab, rows, cols, limit, err, s, launches);
+}
+
+// ---------------------------------------------------------------- root compaction
+
+constexpr int kRootThreads = 256;
+constexpr int kRootItems = 16;                       // per thread
+constexpr int kRootTile = kRootThreads * kRootItems; // elements per block
+
+__device__ __forceinline__ bool is_root(const uint32_t *lab, int64_t i) { return lab[i] == (uint32_t)(i + 1); }
+
+__global__ void k_roots_count(const uint32_t *__restrict__ lab, int64_t n, unsigned *counts) {
+    __shared__ unsigned wsum[kRootThreads / 32];
+    const int64_t base = (int64_t)blockIdx.x * kRootTile;
+    unsigned c = 0;
+#pragma unroll
+    for (int k = 0; k < kRootItems; ++k) {
+        const int64_t i = base + (int64_t)k * kRootThreads + threadIdx.x;
+        if (i < n && is_root(lab, i)) ++c;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+        for (int w = 0; w < kRootThreads / 32; ++w) t += wsum[w];
+        counts[blockIdx.x] = t;
+    }
+}
+
+// Exclusive scan of `nb` block counts in place (one CTA); total -> *total.
+__global__ void k_roots_scan(unsigned *counts, int64_t nb, unsigned long long *total) {
+    __shared__ unsigned long long carry;
+    __shared__ unsigned long long wsum[kRootThreads / 32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t off = 0; off < nb; off += kRootThreads) {
+        const int64_t i = off + threadIdx.x;
+        const unsigned long long v = i < nb ? counts[i] : 0ull;
+        unsigned long long incl = v;
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        unsigned long long wpre = 0;
+        for (int k = 0; k < w; ++k) wpre += wsum[k];
+        const unsigned long long excl = carry + wpre + incl - v;
+        if (i < nb) counts[i] = (unsigned)excl;
+        __syncthreads();
+        if (threadIdx.x == kRootThreads - 1) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// Writes the 1-based index of every root, in increasing order.
+__global__ void k_roots_write(const uint32_t *__restrict__ lab, int64_t n, const unsigned *offsets,
+                              long long *out, int64_t cap) {
+    __shared__ unsigned wsum[kRootThreads / 32];
+    __shared__ unsigned running;
+    const int64_t base = (int64_t)blockIdx.x * kRootTile;
+    if (threadIdx.x == 0) running = offsets[blockIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int k = 0; k < kRootItems; ++k) {
+        const int64_t i = base + (int64_t)k * kRootThreads + threadIdx.x;
+        const bool f = i < n && is_root(lab, i);
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) wsum[w] = __popc(m);
+        __syncthreads();
+        unsigned pre = running;
+        for (int q = 0; q < w; ++q) pre += wsum[q];
+        pre += __popc(m & ((1u << lane) - 1u));
+        if (f && (int64_t)pre < cap) out[pre] = (long long)(i + 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned t = 0;
+            for (int q = 0; q < kRootThreads / 32; ++q) t += wsum[q];
+            running += t;
+        }
+        __syncthreads();
+    }
+}
+
+int64_t roots_blocks(int64_t n) { return (n + kRootTile - 1) / kRootTile; }
+
+cudaError_t roots_count_launch(const uint32_t *lab, int64_t n, unsigned *counts, unsigned long long *total,
+                               cudaStream_t s, int64_t *launches) {
+    const int64_t nb = roots_blocks(n);
+    k_roots_count<<<(unsigned)nb, kRootThreads, 0, s>>>(lab, n, counts);
+    k_roots_scan<<<1, kRootThreads, 0, s>>>(counts, nb, total);
+    *launches += 2;
+    return cudaGetLastError();
+}
+
+cudaError_t roots_write_launch(const uint32_t *lab, int64_t n, const unsigned *offsets, long long *out,
+                               int64_t cap, cudaStream_t s, int64_t *launches) {
+    const int64_t nb = roots_blocks(n);
+    k_roots_write<<<(unsigned)nb, kRootThreads, 0, s>>>(lab, n, offsets, out, cap);
+    *launches += 1;
+    return cudaGetLastError();
+}
+
+}  // namespace ph

@@ -1,0 +1,49 @@
+// ph_ctx.h -- the context object behind the opaque ph_ctx handle.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <list>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+
+
+struct ph_graph_entry {
+    std::string key;
+    cudaGraphExec_t exec = nullptr;
+};
+
+struct ph_ctx {
+    int device = 0;
+    size_t budget = 0;              // 0 = unbounded
+    std::mutex mu;
+    std::string err;
+
+    // twiddle tables W_N^i, i in [0, N), one per transform length
+    std::unordered_map<int, float2 *> tw;
+
+    // scratch arena (grown on demand, never shrunk until destroy)
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+
+    // small fixed device area: [0] loop-limit error flag (int), [8..) 4 doubles of accumulators
+    void *small = nullptr;
+
+    // stream ordering between calls on different streams
+    cudaStream_t last_stream = nullptr;
+    bool has_last = false;
+    cudaEvent_t done = nullptr;
+
+    // private stream used only to record CUDA graphs
+    cudaStream_t capture_stream = nullptr;
+    std::list<ph_graph_entry> graphs;   // most recently used first
+
+    std::atomic<int64_t> launches{0};
+
+    int64_t opt_slice_batch = 0;
+    int64_t opt_use_graphs = 1;
+    int64_t opt_loop_limit = int64_t(1) << 26;
+};

@@ -1,0 +1,201 @@
+// ph_fft.cuh -- the row-FFT engine every pass kernel is built from.
+//
+// A CTA transforms ROWS rows of length N at once.  Each row is handled by
+// P = N/E threads; each thread keeps E complex values in registers and runs
+// radix-E Stockham stages (radix LAST for the trailing stage when N is not a
+// power of E).  Stages exchange data through one padded shared-memory row per
+// transformed row.  The first stage reads its inputs through a caller-supplied
+// `load(slot, col)` and the last stage hands its outputs to `store(slot, col,
+// v)`, so the caller fuses its prologue (transfer multiply, padding, amplitude
+// replacement ...) and epilogue (transposed store, |u|^2, min/argmin, clamp
+// and convert ...) into the transform's first and last register stages.
+//
+// Stockham stage s (radix R, Ns = product of the earlier radices), butterfly b
+// in [0, N/R):   inputs  x[b + r N/R]                     r = 0..R-1
+//               twiddle  x_r *= W_{Ns R}^{r (b mod Ns)}
+//               outputs  y[(b/Ns) Ns R + (b mod Ns) + r Ns]
+// Thread j owns butterflies b = j + m P, m = 0..E/R-1.  In the first and last
+// stage the thread's elements sit at columns b + r N/R (strided by P), which
+// keeps global accesses coalesced across the threads of a row.
+#pragma once
+
+#include "ph_common.cuh"
+
+namespace ph {
+
+template <int N, int E>
+struct FftPlan {
+    static_assert((N & (N - 1)) == 0 && N >= 1, "N must be a power of two");
+    static_assert((E & (E - 1)) == 0 && E >= 1 && E <= N, "E must be a power of two <= N");
+    static constexpr int P = N / E;                       // threads per row
+    static constexpr int LOGN = ilog2c(N);
+    static constexpr int LOGE = ilog2c(E);
+    static constexpr int NFULL = LOGE == 0 ? 0 : LOGN / LOGE;
+    static constexpr int LAST = 1 << (LOGN - NFULL * LOGE);   // trailing radix (1 = none)
+    static constexpr int NSTAGES = NFULL + (LAST > 1 ? 1 : 0);
+    template <int S>
+    __host__ __device__ static constexpr int radix() { return S < NFULL ? E : LAST; }
+    template <int S>
+    __host__ __device__ static constexpr int ns() {   // product of the radices before stage S
+        int v = 1;
+        for (int t = 0; t < S; ++t) v *= (t < NFULL ? E : LAST);
+        return v;
+    }
+};
+
+// Shared-memory index of column i of a row: one pad element per 16 keeps the
+// strided stage writes free of bank conflicts.
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
+
+// Row stride (in float2) of the shared buffer: padded length rounded up to 16,
+// plus 2, so that rows of a CTA fall on different banks when a warp spans rows.
+template <int N>
+struct SmemRow {
+    static constexpr int PADDED = N + (N >> 4);
+    static constexpr int STRIDE = ((PADDED + 15) / 16) * 16 + 2;
+};
+
+// Twiddle of stage twiddle index i for a length-N transform: W_N^i (forward) or
+// its conjugate (inverse).  `tw` holds W_N^i for i in [0, N).
+template <bool INV>
+__device__ __forceinline__ float2 load_tw(const float2 *__restrict__ tw, int i) {
+    float2 w = __ldg(tw + i);
+    if (INV) w.y = -w.y;
+    return w;
+}
+
+// Value the OUT_SMEM variant writes to shared memory: the store callback's result.
+template <bool OUT_SMEM, class Store>
+__device__ __forceinline__ float2 smem_out_value(Store &store, int slot, int col, float2 v) {
+    if constexpr (OUT_SMEM) {
+        return store(slot, col, v);
+    } else {
+        return v;
+    }
+}
+
+// Runs one length-N transform per row.  All threads of the CTA must call it
+// (it synchronises the block).  `srow` is this thread's shared row.
+//
+//   Load:  float2 load(int slot, int col)   -- slot = m*R0 + r (compile-time after unrolling)
+//   Store: void store(int slot, int col, float2 v)
+//   OUT_SMEM: write the outputs to srow (after an internal barrier) and call
+//             store() first so it may transform the value; ends with a barrier.
+//             store() must then RETURN the value to write: float2 store(slot, col, v).
+template <int N, int E, bool INV, bool OUT_SMEM = false, class Load, class Store>
+__device__ __forceinline__ void fft_row(float2 *__restrict__ srow, int j, const float2 *__restrict__ tw,
+                                        Load &&load, Store &&store) {
+    using PL = FftPlan<N, E>;
+    constexpr int P = PL::P;
+    float2 v[E];
+
+    if constexpr (PL::NSTAGES == 0) {
+        // N == 1: identity transform.
+        v[0] = load(0, 0);
+        if constexpr (OUT_SMEM) {
+            __syncthreads();
+            srow[0] = store(0, 0, v[0]);
+            __syncthreads();
+        } else {
+            store(0, 0, v[0]);
+        }
+        return;
+    } else {
+        static_for<PL::NSTAGES>([&](auto SI) {
+            constexpr int S = decltype(SI)::value;
+            constexpr int R = PL::template radix<S>();
+            constexpr int NS = PL::template ns<S>();
+            constexpr int M = E / R;              // butterflies per thread in this stage
+            constexpr int STRIDE_IN = N / R;
+            constexpr bool FIRST = (S == 0);
+            constexpr bool LASTSTAGE = (S == PL::NSTAGES - 1);
+
+            // ---- gather inputs
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int b = j + m * P;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int col = b + r * STRIDE_IN;
+                    if constexpr (FIRST) {
+                        v[m * R + r] = load(m * R + r, col);
+                    } else {
+                        v[m * R + r] = srow[spad(col)];
+                    }
+                }
+            }
+            // ---- twiddle + butterfly
+#pragma unroll
+            for (int m = 0; m < M; ++m) {
+                const int b = j + m * P;
+                float2 t[R];
+#pragma unroll
+                for (int r = 0; r < R; ++r) t[r] = v[m * R + r];
+                if constexpr (NS > 1) {
+                    const int k = b & (NS - 1);
+                    constexpr int TSTEP = N / (NS * R);
+#pragma unroll
+                    for (int r = 1; r < R; ++r) t[r] = cmul(t[r], load_tw<INV>(tw, r * k * TSTEP));
+                }
+                dft<R, INV>(t);
+#pragma unroll
+                for (int r = 0; r < R; ++r) v[m * R + r] = t[r];
+            }
+            // ---- scatter outputs
+            if constexpr (LASTSTAGE && !OUT_SMEM) {
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const int b = j + m * P;   // last stage: (b / NS) == 0, out = b + r*NS
+#pragma unroll
+                    for (int r = 0; r < R; ++r) store(m * R + r, b + r * NS, v[m * R + r]);
+                }
+            } else {
+                __syncthreads();   // every thread has read this stage's inputs
+#pragma unroll
+                for (int m = 0; m < M; ++m) {
+                    const int b = j + m * P;
+                    const int base = (b / NS) * NS * R + (b & (NS - 1));
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const int col = base + r * NS;
+                        if constexpr (LASTSTAGE) {
+                            srow[spad(col)] = smem_out_value<OUT_SMEM>(store, m * R + r, col, v[m * R + r]);
+                        } else {
+                            srow[spad(col)] = v[m * R + r];
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        });
+    }
+}
+
+// Column of output slot `slot` (= m*R + r of the last stage) for thread j.
+template <int N, int E>
+__device__ __forceinline__ int out_col(int j, int slot) {
+    using PL = FftPlan<N, E>;
+    if constexpr (PL::NSTAGES == 0) {
+        return 0;
+    } else {
+        constexpr int R = PL::template radix<PL::NSTAGES - 1>();
+        constexpr int NS = PL::template ns<PL::NSTAGES - 1>();
+        const int m = slot / R, r = slot % R;
+        return j + m * PL::P + r * NS;
+    }
+}
+
+// Column of input slot `slot` (= m*R0 + r of the first stage) for thread j.
+template <int N, int E>
+__device__ __forceinline__ int in_col(int j, int slot) {
+    using PL = FftPlan<N, E>;
+    if constexpr (PL::NSTAGES == 0) {
+        return 0;
+    } else {
+        constexpr int R = PL::template radix<0>();
+        const int m = slot / R, r = slot % R;
+        return j + m * PL::P + r * (N / R);
+    }
+}
+
+}  // namespace ph

@@ -1,0 +1,73 @@
+// ph_launch.cuh -- runtime dispatch from a transform length to the pass kernel
+// compiled for it, and the launch helpers the entry points call.
+#pragma once
+
+#include "ph_passes.cuh"
+
+namespace ph {
+
+// Every supported transform length (powers of two, 1..8192).
+#define PH_FOR_EACH_N(X) \
+    X(1) X(2) X(4) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(8192)
+
+inline bool supported_len(int n) {
+    return n >= 1 && n <= 8192 && (n & (n - 1)) == 0;
+}
+
+// Rows per CTA of the pass compiled for length n.
+inline int rows_per_cta(int n) {
+    switch (n) {
+#define PH_ROWS_CASE(N) case N: return Shape<N>::ROWS;
+        PH_FOR_EACH_N(PH_ROWS_CASE)
+#undef PH_ROWS_CASE
+    }
+    return 0;
+}
+
+template <int N, bool ROW_FAST, class Body>
+cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) {
+    auto kern = k_pass<N, ROW_FAST, Body>;
+    constexpr int smem = Shape<N>::SMEM_BYTES;
+    if constexpr (smem > 48 * 1024) {
+        // Per-device opt-in to more than 48 KB of dynamic shared memory.
+        static unsigned long long done_mask = 0;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const unsigned long long bit = 1ull << (dev & 63);
+        if (!(__atomic_load_n(&done_mask, __ATOMIC_ACQUIRE) & bit)) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            __atomic_fetch_or(&done_mask, bit, __ATOMIC_ACQ_REL);
+        }
+    }
+    dim3 grid((nrows + Shape<N>::ROWS - 1) / Shape<N>::ROWS, grid_y);
+    kern<<<grid, Shape<N>::THREADS, smem, s>>>(body);
+    return cudaGetLastError();
+}
+
+template <bool ROW_FAST, class Body>
+cudaError_t launch_len(int n, const Body &body, int nrows, int grid_y, cudaStream_t s) {
+    switch (n) {
+#define PH_LAUNCH_CASE(N) case N: return launch_one<N, ROW_FAST>(body, nrows, grid_y, s);
+        PH_FOR_EACH_N(PH_LAUNCH_CASE)
+#undef PH_LAUNCH_CASE
+    }
+    return cudaErrorInvalidValue;
+}
+
+// ---- launchers, one translation unit each (compiled in parallel)
+
+cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_COMPLEX> &b, cudaStream_t s);
+cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_SQRT_REAL> &b, cudaStream_t s);
+cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_PADDED> &b, cudaStream_t s);
+cudaError_t launch_spectrum(int n, const SpectrumCols &b, cudaStream_t s);
+cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s);
+cudaError_t launch_recon_b(int n, const ReconB<EPI_PROJ> &b, cudaStream_t s);
+cudaError_t launch_recon_b(int n, const ReconB<EPI_VOL> &b, cudaStream_t s);
+cudaError_t launch_recon_b(int n, const ReconB<EPI_CVOL> &b, cudaStream_t s);
+cudaError_t launch_gs_row(int n, const GsRow<ROW_MID> &b, cudaStream_t s);
+cudaError_t launch_gs_row(int n, const GsRow<ROW_FINAL> &b, cudaStream_t s);
+cudaError_t launch_gs_row(int n, const GsRow<ROW_INV> &b, cudaStream_t s);
+cudaError_t launch_gs_col(int n, const GsCol &b, cudaStream_t s);
+
+}  // namespace ph

@@ -1,0 +1,376 @@
+// ph_passes.cuh -- the pass kernels of the reconstruction, Gerchberg-Saxton and
+// propagation paths.  Every pass reads whole rows (contiguous), transforms them
+// with the row-FFT engine and writes either whole rows or, with the
+// transposed store, columns of the output: two passes make one 2-D transform
+// and the transpose between them costs nothing extra.
+//
+// Layouts (n_fast = nx, n_slow = ny):
+//   image-domain arrays       [ny][nx]   (wavefront, holograms, projection, slices)
+//   transfer functions        [ny][nx]   centred (fftshifted), as the caller builds them
+//   after a forward row pass  [nx][ny]   (row = kx, along y)
+//   spectrum state            [nx][ny]   float4 (re, im, phase-rate bits, |Hdz|-1)
+//   slice intermediate T      [batch][ny][nx]
+#pragma once
+
+#include <cuda_fp16.h>
+#include "ph_fft.cuh"
+
+namespace ph {
+
+// ---------------------------------------------------------------- launch shape
+
+template <int N>
+struct Shape {
+    static constexpr int E = N < 16 ? N : 16;
+    static constexpr int P = N / E;
+    static constexpr int ROWS = cmax(1, cmin(64, 512 / P));
+    static constexpr int THREADS = ROWS * P;
+    static constexpr int SMEM_BYTES = ROWS * SmemRow<N>::STRIDE * 8;
+};
+
+template <int N, bool ROW_FAST>
+struct ThreadMap {
+    __device__ __forceinline__ static int row(int t) { return ROW_FAST ? t % Shape<N>::ROWS : t / Shape<N>::P; }
+    __device__ __forceinline__ static int j(int t) { return ROW_FAST ? t / Shape<N>::ROWS : t % Shape<N>::P; }
+};
+
+template <int N, bool ROW_FAST, class Body>
+__global__ void __launch_bounds__(Shape<N>::THREADS) k_pass(const Body body) {
+    extern __shared__ float2 ph_smem[];
+    const int t = threadIdx.x;
+    const int r = ThreadMap<N, ROW_FAST>::row(t);
+    const int j = ThreadMap<N, ROW_FAST>::j(t);
+    body.template run<N>(ph_smem + r * SmemRow<N>::STRIDE, r, j);
+}
+
+__device__ __forceinline__ int shift_idx(int i, int n) {   // centred index of natural frequency i
+    int s = i + (n >> 1);
+    return s >= n ? s - n : s;
+}
+
+// ---------------------------------------------------------------- forward rows (transposed store)
+
+enum FwdInput { FWD_COMPLEX = 0, FWD_SQRT_REAL = 1, FWD_PADDED = 2 };
+
+// out[kx][y] = FFT_x(in[y][:])[kx].  FWD_SQRT_REAL: in = sqrtf(real[y][x]) + 0i.
+// FWD_PADDED: the input is the virtual 2n x 2n mean-padded array of `src`
+// (n = nx_in) with `src` at rows/cols [pad_off, pad_off + n).
+template <int MODE>
+struct FwdRowsT {
+    const float2 *src;
+    const float *src_real;
+    float2 *dst;
+    const float2 *tw;
+    const float2 *pad_mean;   // device scalar (FWD_PADDED)
+    int nrows;                // rows of the (virtual) input = ny
+    int nx_in, ny_in, pad_off;
+
+    template <int N>
+    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+        const int y = blockIdx.x * Shape<N>::ROWS + r;
+        const bool valid = y < nrows;
+        float2 mean = make_float2(0.f, 0.f);
+        if (MODE == FWD_PADDED) mean = *pad_mean;
+        fft_row<N, Shape<N>::E, false>(
+            srow, j, tw,
+            [&](int, int x) -> float2 {
+                if (!valid) return make_float2(0.f, 0.f);
+                if constexpr (MODE == FWD_COMPLEX) {
+                    return src[(size_t)y * N + x];
+                } else if constexpr (MODE == FWD_SQRT_REAL) {
+                    return make_float2(sqrtf(src_real[(size_t)y * N + x]), 0.f);
+                } else {
+                    const int yi = y - pad_off, xi = x - pad_off;
+                    if (yi >= 0 && yi < ny_in && xi >= 0 && xi < nx_in) return src[(size_t)yi * nx_in + xi];
+                    return mean;
+                }
+            },
+            [&](int, int kx, float2 v) {
+                if (valid) dst[(size_t)kx * nrows + y] = v;
+            });
+    }
+};
+
+// ---------------------------------------------------------------- spectrum state
+
+// Phase of h as a 32-bit fixed-point fraction of a turn (FP64 atan2).
+__device__ __forceinline__ uint32_t phase_turns_u32(float2 h) {
+    const double a = atan2((double)h.y, (double)h.x) * 0.15915494309189533577;   // / 2 pi
+    const long long q = __double2ll_rn(a * 4294967296.0);
+    return (uint32_t)(unsigned long long)q;
+}
+
+// Rows kx of the forward-row output, FFT along y, times the front transfer
+// (and 1/(nx ny)), stored with the slice phase rate of the slice transfer:
+// state[kx][ky] = (X0, turns(Hdz), |Hdz| - 1).
+struct SpectrumCols {
+    const float2 *a1;        // [nx][ny]
+    const float2 *hf, *hdz;  // centred [ny][nx]
+    float4 *state;           // [nx][ny]
+    const float2 *tw;
+    int nx, ny;
+    float scale;
+
+    template <int N>
+    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+        const int kx = blockIdx.x * Shape<N>::ROWS + r;
+        const bool valid = kx < nx;
+        const int sx = valid ? shift_idx(kx, nx) : 0;
+        fft_row<N, Shape<N>::E, false>(
+            srow, j, tw,
+            [&](int, int y) -> float2 { return valid ? a1[(size_t)kx * N + y] : make_float2(0.f, 0.f); },
+            [&](int, int ky, float2 v) {
+                if (!valid) return;
+                const size_t c = (size_t)shift_idx(ky, N) * nx + sx;
+                const float2 x0 = cscale(cmul(v, hf[c]), scale);
+                const float2 d = hdz[c];
+                const float mag_m1 = (float)(sqrt((double)d.x * d.x + (double)d.y * d.y) - 1.0);
+                state[(size_t)kx * N + ky] = make_float4(x0.x, x0.y, __uint_as_float(phase_turns_u32(d)), mag_m1);
+            });
+    }
+};
+
+// ---------------------------------------------------------------- reconstruction pass A
+
+// Slice k of rows kx: X_k = X0 * Hdz^k evaluated directly from the phase rate
+// (exact integer turn arithmetic) and |Hdz|^k ~ 1 + k (|Hdz| - 1); inverse FFT
+// along ky; transposed store T[b][y - y0][kx] for y in [y0, y0 + ny_out).
+struct ReconA {
+    const float4 *state;   // [nx][ny]
+    float2 *t;             // [batch][ny_out][nx]
+    const float2 *tw;
+    int nx, ny_out, y0;
+    int k0;                // global slice index of batch slot 0
+
+    template <int N>
+    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+        const int kx = blockIdx.x * Shape<N>::ROWS + r;
+        const bool valid = kx < nx;
+        const int b = blockIdx.y;
+        const uint32_t k = (uint32_t)(k0 + b);
+        const float kf = (float)k;
+        float2 *tb = t + (size_t)b * ny_out * nx;
+        fft_row<N, Shape<N>::E, true>(
+            srow, j, tw,
+            [&](int, int ky) -> float2 {
+                if (!valid) return make_float2(0.f, 0.f);
+                const float4 s = state[(size_t)kx * N + ky];
+                const int32_t tt = (int32_t)(k * __float_as_uint(s.z));
+                const float ang = (float)tt * 1.46291807926715968e-9f;   // 2 pi / 2^32
+                float sn, cs;
+                __sincosf(ang, &sn, &cs);
+                const float mag = fmaf(kf, s.w, 1.0f);
+                const float2 g = make_float2(cs * mag, sn * mag);
+                return cmul(make_float2(s.x, s.y), g);
+            },
+            [&](int, int y, float2 v) {
+                const int yo = y - y0;
+                if (valid && yo >= 0 && yo < ny_out) tb[(size_t)yo * nx + kx] = v;
+            });
+    }
+};
+
+// ---------------------------------------------------------------- reconstruction pass B
+
+enum Epilogue {
+    EPI_PROJ = 0,      // running min / argmin -> packed atomicMin
+    EPI_VOL = 1,       // clamp + convert -> vol (optionally the min of the stored values)
+    EPI_CVOL = 2       // complex slice -> vol
+};
+
+__device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
+
+// Rows y of T, inverse FFT along kx, |u|^2 and the epilogue.  A CTA handles
+// ROWS rows for `group` consecutive batch slots; with EPI_PROJ the running
+// minimum stays in registers across them and is merged with one atomicMin of
+// (float bits << 32 | slice) per pixel.
+template <int EPI>
+struct ReconB {
+    const float2 *t;                 // [batch][rows][nx]
+    const float2 *tw;
+    unsigned long long *proj64;      // [rows_out][nx_out] or null
+    void *vol;                       // [S][rows_out][nx_out] or null
+    int vol_dtype;
+    int rows;                        // rows of T per slice
+    int nx_out, x0;                  // stored columns [x0, x0 + nx_out)
+    int k0, nbatch, group;
+    long long vol_slice_stride;      // elements per stored slice
+
+    template <int N>
+    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+        constexpr int E = Shape<N>::E;
+        const int y = blockIdx.x * Shape<N>::ROWS + r;
+        const bool valid = y < rows;
+        const int b0 = blockIdx.y * group;
+        const int b1 = min(b0 + group, nbatch);
+        float minv[E];
+        int mink[E];
+#pragma unroll
+        for (int s = 0; s < E; ++s) { minv[s] = __int_as_float(0x7f800000); mink[s] = 0; }
+        const bool track_min = (EPI == EPI_PROJ) || (EPI == EPI_VOL && proj64 != nullptr);
+
+        for (int b = b0; b < b1; ++b) {
+            const int k = k0 + b;
+            const float2 *tb = t + ((size_t)b * rows + (valid ? y : 0)) * N;
+            fft_row<N, E, true>(
+                srow, j, tw,
+                [&](int, int kx) -> float2 { return valid ? tb[kx] : make_float2(0.f, 0.f); },
+                [&](int slot, int x, float2 v) {
+                    if constexpr (EPI == EPI_PROJ) {
+                        const float in = fmaf(v.x, v.x, v.y * v.y);
+                        if (in < minv[slot]) { minv[slot] = in; mink[slot] = k; }
+                    } else {
+                        const int xo = x - x0;
+                        if (!valid || xo < 0 || xo >= nx_out) return;
+                        const size_t o = (size_t)k * vol_slice_stride + (size_t)y * nx_out + xo;
+                        if constexpr (EPI == EPI_CVOL) {
+                            reinterpret_cast<float2 *>(vol)[o] = v;
+                        } else {
+                            const float in = clamp01(fmaf(v.x, v.x, v.y * v.y));
+                            float stored;
+                            switch (vol_dtype) {
+                                case 0: {   // N0f8
+                                    const unsigned q = __float2uint_rn(in * 255.0f);
+                                    reinterpret_cast<uint8_t *>(vol)[o] = (uint8_t)q;
+                                    stored = __fdiv_rn((float)q, 255.0f);
+                                    break;
+                                }
+                                case 1: {
+                                    const __half h = __float2half_rn(in);
+                                    reinterpret_cast<__half *>(vol)[o] = h;
+                                    stored = __half2float(h);
+                                    break;
+                                }
+                                case 3:
+                                    reinterpret_cast<double *>(vol)[o] = (double)in;
+                                    stored = in;
+                                    break;
+                                default:
+                                    reinterpret_cast<float *>(vol)[o] = in;
+                                    stored = in;
+                                    break;
+                            }
+                            if (track_min && stored < minv[slot]) { minv[slot] = stored; mink[slot] = k; }
+                        }
+                    }
+                });
+        }
+        if (track_min && valid) {
+#pragma unroll
+            for (int s = 0; s < E; ++s) {
+                const int x = out_col<N, E>(j, s);
+                const int xo = x - x0;
+                if (xo >= 0 && xo < nx_out && b1 > b0)
+                    atomicMin(proj64 + (size_t)y * nx_out + xo, pack_min(minv[s], mink[s]));
+            }
+        }
+    }
+};
+
+// ---------------------------------------------------------------- Gerchberg-Saxton / propagation
+
+enum RowMode {
+    ROW_MID = 0,      // inverse FFT -> amplitude replace -> forward FFT -> transposed store
+    ROW_FINAL = 1,    // inverse FFT -> amplitude replace -> natural store
+    ROW_INV = 2,      // inverse FFT -> natural store
+};
+
+__device__ __forceinline__ float2 amplitude_replace(float2 u, float s) {
+    if (u.x == 0.0f && u.y == 0.0f) return make_float2(s, 0.0f);   // angle(0) == 0
+    const float inv = rhypotf(u.x, u.y);
+    return make_float2(u.x * inv * s, u.y * inv * s);
+}
+
+// Rows y of [y][kx] data (row length nx).
+template <int MODE>
+struct GsRow {
+    const float2 *src;       // [ny][nx]
+    const float *holo;       // [ny][nx] intensity whose sqrt replaces the amplitude
+    float2 *dst;             // MID: [nx][ny]; FINAL / INV: [ny][nx]
+    const float2 *tw;
+    double *resid;           // nullable: [0] += (|u| - s)^2, [1] += s^2
+    int nrows;
+
+    template <int N>
+    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+        constexpr int E = Shape<N>::E;
+        const int y = blockIdx.x * Shape<N>::ROWS + r;
+        const bool valid = y < nrows;
+        const float2 *in = src + (size_t)(valid ? y : 0) * N;
+        auto ld = [&](int, int x) -> float2 { return valid ? in[x] : make_float2(0.f, 0.f); };
+        if constexpr (MODE == ROW_INV) {
+            fft_row<N, E, true>(srow, j, tw, ld, [&](int, int x, float2 v) {
+                if (valid) dst[(size_t)y * N + x] = v;
+            });
+        } else if constexpr (MODE == ROW_FINAL) {
+            fft_row<N, E, true>(srow, j, tw, ld, [&](int, int x, float2 v) {
+                if (valid) dst[(size_t)y * N + x] = amplitude_replace(v, sqrtf(holo[(size_t)y * N + x]));
+            });
+        } else {
+            double acc0 = 0.0, acc1 = 0.0;
+            fft_row<N, E, true, true>(srow, j, tw, ld, [&](int, int x, float2 v) -> float2 {
+                if (!valid) return make_float2(0.f, 0.f);
+                const float s = sqrtf(holo[(size_t)y * N + x]);
+                if (resid != nullptr) {
+                    const double a = sqrt((double)v.x * v.x + (double)v.y * v.y) - (double)s;
+                    acc0 += a * a;
+                    acc1 += (double)s * s;
+                }
+                return amplitude_replace(v, s);
+            });
+            fft_row<N, E, false>(
+                srow, j, tw, [&](int, int x) -> float2 { return srow[spad(x)]; },
+                [&](int, int kx, float2 v) {
+                    if (valid) dst[(size_t)kx * nrows + y] = v;
+                });
+            if (resid != nullptr) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
+                    acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
+                }
+                if ((threadIdx.x & 31) == 0) {
+                    atomicAdd(resid, acc0);
+                    atomicAdd(resid + 1, acc1);
+                }
+            }
+        }
+    }
+};
+
+// Rows kx of [kx][y] data (row length ny): forward FFT along y, times the
+// centred transfer (and `scale`), inverse FFT along y, transposed store [y][kx].
+// With `mask` (real, centred) instead of `h`, the multiplier is the mask.
+struct GsCol {
+    const float2 *src;       // [nx][ny]
+    const float2 *h;         // centred [ny][nx] (or null)
+    const float *mask;       // centred [ny][nx] (or null)
+    float2 *dst;             // [ny][nx]
+    const float2 *tw;
+    int nx;
+    float scale;
+
+    template <int N>
+    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+        constexpr int E = Shape<N>::E;
+        const int kx = blockIdx.x * Shape<N>::ROWS + r;
+        const bool valid = kx < nx;
+        const int sx = valid ? shift_idx(kx, nx) : 0;
+        const float2 *in = src + (size_t)(valid ? kx : 0) * N;
+        fft_row<N, E, false, true>(
+            srow, j, tw, [&](int, int y) -> float2 { return valid ? in[y] : make_float2(0.f, 0.f); },
+            [&](int, int ky, float2 v) -> float2 {
+                if (!valid) return make_float2(0.f, 0.f);
+                const size_t c = (size_t)shift_idx(ky, N) * nx + sx;
+                if (mask != nullptr) return cscale(v, mask[c] * scale);
+                return cscale(cmul(v, h[c]), scale);
+            });
+        fft_row<N, E, true>(
+            srow, j, tw, [&](int, int ky) -> float2 { return srow[spad(ky)]; },
+            [&](int, int y, float2 v) {
+                if (valid) dst[(size_t)y * nx + kx] = v;
+            });
+    }
+};
+
+}  // namespace ph

@@ -1,0 +1,76 @@
+"""The C ABI boundary (no GPU): the library loads, exports every symbol that
+include/phgb300.h declares, and every declaration names the reference function
+it replaces or says it has no counterpart."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "phgb300.h"
+
+
+def _declared():
+    text = HEADER.read_text()
+    return re.findall(r"^PH_API\s+[\w\s\*]+?\b(ph_\w+)\s*\(", text, flags=re.M)
+
+
+def test_header_declares_entry_points():
+    names = _declared()
+    assert len(names) >= 20
+    for must in ("ph_reconst_xyproj", "ph_reconst_vol", "ph_phase_retrieval", "ph_ccl", "ph_ccl_roots",
+                 "ph_transfer", "ph_transfer_sqrt", "ph_asm_prop", "ph_reconst_vol_padded", "ph_pad2d"):
+        assert must in names
+
+
+def test_library_loads_and_exports_every_symbol(ph):
+    from ph_gb300 import _lib
+    lib = _lib.lib()
+    assert lib.ph_version() >= 100
+    for name in _declared():
+        assert hasattr(lib, name), f"{name} declared in phgb300.h but not exported"
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+    assert set(_lib.SIGNATURES) == set(_declared())
+
+
+def test_every_declaration_cites_reference():
+    text = HEADER.read_text()
+    blocks = re.split(r"\n(?=/\*)", text)
+    for name in _declared():
+        if name in ("ph_create", "ph_destroy", "ph_last_error", "ph_version", "ph_set_option",
+                    "ph_scratch_bytes", "ph_reserve", "ph_kernel_launches"):
+            continue
+        block = next(b for b in blocks if re.search(rf"\b{name}\s*\(", b))
+        assert re.search(r"\.jl:\d+", block) or "No reference counterpart" in block or "no counterpart" in block, name
+
+
+def test_null_context_is_rejected(ph):
+    from ph_gb300 import _lib
+    lib = _lib.lib()
+    assert lib.ph_reconst_xyproj(None, None, None, None, None, None, 8, 8, 1, None) == _lib.PH_ERR_INVALID
+    assert lib.ph_set_option(None, 1, 1) == _lib.PH_ERR_INVALID
+    assert lib.ph_last_error(None) == b"null context"
+
+
+def test_create_without_gpu_fails_cleanly(ph):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from ph_gb300 import _lib
+    h = ctypes.c_void_p()
+    assert _lib.lib().ph_create(0, 0, ctypes.byref(h)) == _lib.PH_ERR_CUDA
+    assert not h.value
+
+
+def test_host_mirror_validates_before_launch(ph):
+    """Size and dtype checks happen on the host with the reference's messages."""
+    import torch
+    a = torch.zeros((4, 4), dtype=torch.complex64)
+    b = torch.zeros((8, 8), dtype=torch.complex64)
+    with pytest.raises(AssertionError, match="All arrays must have the same size. Got \\(4, 4\\), \\(8, 8\\)"):
+        ph.cu_get_reconst_xyprojection(ph.CuWavefront(a), ph.CuTransfer(b), ph.CuTransfer(a), 2)
+    with pytest.raises(TypeError):
+        ph.cu_get_reconst_xyprojection(ph.CuWavefront(a.real.contiguous()), ph.CuTransfer(a), ph.CuTransfer(a), 2)
+    with pytest.raises(AssertionError, match="2\\*size"):
+        ph.cu_get_reconst_vol_and_xyprojection_padded(ph.CuWavefront(a), ph.CuTransfer(a), ph.CuTransfer(a), 2)

@@ -1,0 +1,103 @@
+"""Connected-component labeling on the GPU: bit-exact against the C oracle
+(ccl.jl:13-238) and the reference's known answer (84 components)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import ccl as occl
+from oracle import ref_semantics as ref
+from phtest import to_dev, to_np
+
+pytestmark = pytest.mark.gpu
+
+
+def _labels(ph, img_np, cuda, **kw):
+    return to_np(ph.cu_connected_component_labeling(to_dev(img_np, cuda), **kw)).astype(np.uint32)
+
+
+def test_binaryparticles_84(ph, cuda, golden):
+    g = golden("binaryparticles")
+    img = np.unpackbits(g["fg_bits"])[: int(np.prod(g["shape"]))].reshape(g["shape"]).astype(np.float32)
+    lab_t = ph.cu_connected_component_labeling(to_dev(img, cuda))
+    assert tuple(lab_t.shape) == (1024, 1024)
+    lab = to_np(lab_t).astype(np.uint32)
+    assert np.array_equal(lab, occl.connected_component_labeling(img))
+    assert ph.count_labels(lab_t) == 84                      # runtests.jl:217
+    valid = ph.cu_find_valid_labels(lab_t)
+    assert valid.dtype == np.int64 and len(valid) == 84       # runtests.jl:231
+    assert np.array_equal(valid, ref.find_valid_labels(lab))
+    # Bool input gives the same labels
+    lab_b = to_np(ph.cu_connected_component_labeling(to_dev(img > 0, cuda))).astype(np.uint32)
+    assert np.array_equal(lab_b, lab)
+
+
+@pytest.mark.parametrize("shape,levels,p", [((1, 1), 2, 0.5), ((1, 37), 2, 0.5), ((37, 1), 2, 0.5),
+                                            ((64, 64), 2, 0.45), ((64, 64), 4, 0.5), ((256, 256), 2, 0.6),
+                                            ((1024, 1024), 2, 0.5), ((2048, 2048), 2, 0.3)])
+def test_random_images_bit_exact(ph, cuda, shape, levels, p):
+    rng = np.random.default_rng(shape[0] * 7 + levels)
+    if levels == 2:
+        img = (rng.random(shape) < p).astype(np.float32)
+    else:
+        img = rng.integers(0, levels, shape).astype(np.float32)
+    assert np.array_equal(_labels(ph, img, cuda), occl.connected_component_labeling(img))
+
+
+def test_golden_multivalued(ph, cuda, golden):
+    g = golden("oracle_small")
+    for k in range(3):
+        assert np.array_equal(_labels(ph, g[f"ccl{k}_img"], cuda), g[f"ccl{k}_lab"])
+
+
+@pytest.mark.parametrize("shape", [(24, 40), (40, 24)])
+def test_rectangular_grids(ph, cuda, shape):
+    rng = np.random.default_rng(5)
+    img = (rng.random(shape) < 0.5).astype(np.float32)
+    n_slow, n_fast = shape
+    # the reference's grid: rows = size(img,1) = n_fast over the linear buffer
+    want_ref = occl.connected_component_labeling(img, rows=n_fast, cols=n_slow)
+    assert np.array_equal(_labels(ph, img, cuda).reshape(-1), want_ref.reshape(-1))
+    # the true 2-D image
+    want_2d = occl.connected_component_labeling(img)
+    assert np.array_equal(_labels(ph, img, cuda, reference_grid=False), want_2d)
+
+
+def test_snake_long_chains(ph, cuda):
+    """A single serpentine component exercises long union chains."""
+    n = 512
+    img = np.zeros((n, n), np.float32)
+    img[::2, :] = 1
+    img[1::4, -1] = 1
+    img[3::4, 0] = 1
+    lab = _labels(ph, img, cuda)
+    assert np.array_equal(lab, occl.connected_component_labeling(img))
+    assert ref.count_labels(lab) == 1
+
+
+def test_loop_limit_reports_timeout(ph, cuda):
+    """With an iteration limit of 1 the bounded chase gives up and the host sees PH_ERR_TIMEOUT."""
+    from ph_gb300 import _lib
+    ctx = _lib.default_context(0)
+    n = 256
+    img = np.zeros((n, n), np.float32)
+    img[::2, :] = 1
+    img[1::4, -1] = 1
+    img[3::4, 0] = 1
+    try:
+        ctx.set_option(_lib.PH_OPT_LOOP_LIMIT, 1)
+        lab = ph.cu_connected_component_labeling(to_dev(img, cuda))
+        with pytest.raises(_lib.PhError, match="iteration limit"):
+            ph.count_labels(lab)
+    finally:
+        ctx.set_option(_lib.PH_OPT_LOOP_LIMIT, 1 << 26)
+    lab = ph.cu_connected_component_labeling(to_dev(img, cuda))
+    assert ph.count_labels(lab) == 1
+
+
+def test_deterministic(ph, cuda):
+    rng = np.random.default_rng(0)
+    img = (rng.random((512, 512)) < 0.55).astype(np.float32)
+    t = to_dev(img, cuda)
+    first = to_np(ph.cu_connected_component_labeling(t))
+    for _ in range(20):
+        assert np.array_equal(to_np(ph.cu_connected_component_labeling(t)), first)
