@@ -1,0 +1,432 @@
+"""Benchmark of the reconstruction hot path on GB300 (one JSON line on stdout).
+
+Workload (default, ``--config c2``): a seeded pair of 2048 x 2048 Float32
+holograms (800 opaque discs, diameter 10-60 um, z in [5, 100] mm, recorded
+5 mm apart, lambda = 0.6328 um, pitch 10 um).  One step is one frame:
+Gerchberg-Saxton phase retrieval (20 iterations) -> angular-spectrum
+reconstruction of 512 slices at dz = 0.2 mm from z0 = 5 mm reduced on the fly to
+the xy min-projection and argmin-depth map -> threshold -> connected-component
+labeling.  Metric: reconstructed Mvoxel/s (voxel = one pixel of one slice),
+with p50/p99 frame latency.
+
+``value``  device-resident inputs, CUDA events per step on the launching stream,
+          L2 flushed (a 512 MiB write) before every timed step, outside the events.
+``e2e``    the same frame through the public API from pinned host buffers: the
+          hologram pair copied in, projection + argmin copied out and the
+          component count read back, every step.
+``roofline`` the dominant kernel's algorithmic bytes per launch over its
+          CUDA-event duration (library profiler, on the launching stream,
+          during the timed steps).
+``cpu_baseline`` the oracle (numpy / scipy.fft on all host cores, FP32) timed
+          on a bounded sample of the frame and scaled to Mvoxel/s.
+``--impl reference`` times that CPU path as the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+LAM, DX = 0.6328, 10.0
+CONFIGS = {
+    # name: (n, slices, dz, z0, discs, dmin, dmax, zmin, zmax, gs_iters, gs_sep, threshold, seed)
+    "c1": dict(n=1024, slices=256, dz=200.0, z0=1000.0, discs=200, dmin=20.0, dmax=80.0, zmin=1000.0,
+               zmax=50000.0, gs_iters=0, gs_sep=0.0, threshold=0.5, seed=1,
+               workload="gabor1024_recon256_ccl"),
+    "c2": dict(n=2048, slices=512, dz=200.0, z0=5000.0, discs=800, dmin=10.0, dmax=60.0, zmin=5000.0,
+               zmax=100000.0, gs_iters=20, gs_sep=5000.0, threshold=0.1, seed=2,
+               workload="gs2048_pr20_recon512_proj_argmin_ccl"),
+    "c3": dict(n=4096, slices=1024, dz=(200000.0 - 5000.0) / 1024, z0=5000.0, discs=3000, dmin=10.0, dmax=60.0,
+               zmin=5000.0, zmax=200000.0, gs_iters=0, gs_sep=0.0, threshold=0.1, seed=3,
+               workload="gabor4096_recon1024_ccl"),
+}
+L2_FLUSH_BYTES = 512 << 20
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- algorithmic bytes per launch
+
+def algorithmic_bytes(name: str, cfg: dict, launches: int, slices_per_frame: int) -> float | None:
+    """Bytes one launch of `name` must move through DRAM by design, per launch.
+
+    recon_a  writes the slice intermediate T: 8 B per voxel (the spectrum state it
+             reads, 16 B per pixel, stays resident in L2 across the batch).
+    recon_b  reads T: 8 B per voxel.
+    gs_col   reads and writes the field: 16 B per pixel.
+    gs_row_* reads and writes the field (16 B) and reads the hologram (4 B).
+    fwd_rows / spectrum: 8 + 8 B and 8 + 16 (+16 transfer reads) B per pixel.
+    """
+    n2 = cfg["n"] ** 2
+    per_frame = {
+        "recon_a": 8.0 * n2 * slices_per_frame,
+        "recon_b": 8.0 * n2 * slices_per_frame,
+    }
+    if name in per_frame:
+        return per_frame[name] / max(1, launches)
+    per_launch = {"gs_col": 16.0 * n2 + 16.0 * n2, "gs_row_mid": 20.0 * n2, "gs_row_final": 20.0 * n2,
+                  "fwd_rows": 16.0 * n2, "spectrum": 8.0 * n2 + 16.0 * n2 + 16.0 * n2}
+    return per_launch.get(name)
+
+
+# ---------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"ph_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        self.path.unlink(missing_ok=True)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU (oracle) frame sample
+
+def cpu_frame_sample(cfg: dict, h1: np.ndarray, h2: np.ndarray, gs_iters: int, slices: int):
+    """Times the oracle on `gs_iters` GS iterations, `slices` slices and one labeling;
+    returns (seconds per GS iteration, seconds per slice, seconds per labeling)."""
+    from oracle import ccl as occl
+    from oracle import ref_semantics as ref
+    n = cfg["n"]
+    d = ref.transfer_sqrt_arr(n, LAM, DX)
+    hf, hdz = ref.transfer(-cfg["z0"], n, LAM, d), ref.transfer(-cfg["dz"], n, LAM, d)
+    t_it = 0.0
+    if cfg["gs_iters"] > 0 and gs_iters > 0:
+        tp, tpi = ref.transfer(cfg["gs_sep"], n, LAM, d), ref.transfer(-cfg["gs_sep"], n, LAM, d)
+        t = time.perf_counter()
+        wf = ref.phase_retrieval_holo(h1, h2, tp, tpi, gs_iters, n)
+        t_it = (time.perf_counter() - t) / gs_iters
+    else:
+        wf = ref.gabor_wavefront(h1)
+    t = time.perf_counter()
+    proj = ref.reconst_xyprojection(wf, hf, hdz, slices)
+    t_slice = (time.perf_counter() - t) / slices
+    t = time.perf_counter()
+    occl.connected_component_labeling((proj <= cfg["threshold"]).astype(np.float32))
+    t_ccl = time.perf_counter() - t
+    return t_it, t_slice, t_ccl
+
+
+def cpu_mvoxel_per_s(cfg, t_it, t_slice, t_ccl) -> float:
+    frame = cfg["gs_iters"] * t_it + cfg["slices"] * t_slice + t_ccl
+    return cfg["n"] ** 2 * cfg["slices"] / frame / 1e6
+
+
+# ---------------------------------------------------------------- main
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-profile", action="store_true")
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return reference_arm(args, cfg, rank, world)
+
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+
+    import __graft_entry__ as g
+    ph = g.load_package()
+    from ph_gb300 import _lib, synth
+
+    n, S = cfg["n"], cfg["slices"]
+    ctx = _lib.default_context(local)
+    # ---- inputs (seeded, synthesised on the device, then kept on the host too)
+    spec = synth.HologramSpec(seed=cfg["seed"] + 1000 * rank, n=n, count=cfg["discs"], dmin=cfg["dmin"],
+                              dmax=cfg["dmax"], zmin=cfg["zmin"], zmax=cfg["zmax"], wavlen=LAM, dx=DX)
+    if cfg["gs_iters"] > 0:
+        h1, h2 = synth.synth_pair(spec, cfg["gs_sep"], local)
+    else:
+        h1 = synth.synth_hologram(spec, local)
+        h2 = h1
+    d_sqr = ph.cu_transfer_sqrt_arr(n, LAM, DX, device=local)
+    hf = ph.cu_transfer(-cfg["z0"], n, LAM, d_sqr)
+    hdz = ph.cu_transfer(-cfg["dz"], n, LAM, d_sqr)
+    hp = ph.cu_transfer(cfg["gs_sep"], n, LAM, d_sqr)
+    hpi = ph.cu_transfer(-cfg["gs_sep"], n, LAM, d_sqr)
+    h1_host = torch.empty(h1.shape, dtype=torch.float32, pin_memory=True)
+    h2_host = torch.empty(h2.shape, dtype=torch.float32, pin_memory=True)
+    h1_host.copy_(h1)
+    h2_host.copy_(h2)
+    proj_host = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
+    arg_host = torch.empty((n, n), dtype=torch.int32, pin_memory=True)
+    wf = torch.empty((n, n), dtype=torch.complex64, device=dev)
+    proj = torch.empty((n, n), dtype=torch.float32, device=dev)
+    arg = torch.empty((n, n), dtype=torch.int32, device=dev)
+    binary = torch.empty((n, n), dtype=torch.uint8, device=dev)
+    labels = torch.empty((n, n), dtype=torch.int32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    s = stream.cuda_stream
+
+    def frame(in1, in2):
+        if cfg["gs_iters"] > 0:
+            ctx.call("ph_phase_retrieval", wf.data_ptr(), in1.data_ptr(), in2.data_ptr(), hp.data.data_ptr(),
+                     hpi.data.data_ptr(), n, n, cfg["gs_iters"], None, s)
+        else:
+            ctx.call("ph_gabor_wavefront", wf.data_ptr(), in1.data_ptr(), n, n, s)
+        ctx.call("ph_reconst_xyproj", proj.data_ptr(), arg.data_ptr(), wf.data_ptr(), hf.data.data_ptr(),
+                 hdz.data.data_ptr(), n, n, S, s)
+        ctx.call("ph_binarize_le", binary.data_ptr(), proj.data_ptr(), n * n, float(cfg["threshold"]), s)
+        ctx.call("ph_ccl", labels.data_ptr(), binary.data_ptr(), _lib.PH_BOOL, n, n, s)
+
+    # ---- device-resident timing
+    for _ in range(args.warmup):
+        frame(h1, h2)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if not args.no_profile:
+        ctx.set_option(_lib.PH_OPT_PROFILE, 1)
+        ctx.profile_report()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = ctx.launches
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.zero_()                     # L2 flush, outside the step's events
+        ev[i][0].record(stream)
+        frame(h1, h2)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches - l0
+    clk = clocks.stop()
+    prof = ctx.profile_report() if not args.no_profile else {}
+    ctx.set_option(_lib.PH_OPT_PROFILE, 0)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = float(sum(step_ms))
+    t = torch.tensor([total_ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    voxels = n * n * S
+    value = voxels * args.steps * world / (total_ms / 1e3) / 1e6
+
+    # ---- end to end through the public API, host buffers
+    e2e = None
+    if not args.no_e2e:
+        d1 = torch.empty_like(h1)
+        d2 = torch.empty_like(h2)
+
+        def e2e_frame():
+            d1.copy_(h1_host, non_blocking=True)
+            d2.copy_(h2_host, non_blocking=True)
+            if cfg["gs_iters"] > 0:
+                u = ph.cu_phase_retrieval_holo(d1, d2, hp, hpi, cfg["gs_iters"], n)
+            else:
+                u = ph.cu_gabor_wavefront(d1)
+            p, a = ph.cu_get_reconst_xyprojection(u, hf, hdz, S, return_argmin=True)
+            ctx.call("ph_binarize_le", binary.data_ptr(), p.data_ptr(), n * n, float(cfg["threshold"]), s)
+            lab = ph.cu_connected_component_labeling(binary)
+            proj_host.copy_(p, non_blocking=True)
+            arg_host.copy_(a, non_blocking=True)
+            return ph.count_labels(lab)       # reads the count back (synchronises)
+
+        for _ in range(max(1, args.warmup)):
+            e2e_frame()
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        e_ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ncomp = e2e_frame()
+            torch.cuda.synchronize()
+            e_ms.append((time.perf_counter() - t0) * 1e3)
+        te = torch.tensor([sum(e_ms)], device=dev)
+        if world > 1:
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        e2e = {"value": round(voxels * args.steps * world / (float(te.item()) / 1e3) / 1e6, 2), "unit": "Mvoxel/s",
+               "h2d_bytes_per_step": int(h1.numel() * 4 * (2 if cfg["gs_iters"] > 0 else 1)),
+               "d2h_bytes_per_step": int(proj.numel() * 4 + arg.numel() * 4 + 8),
+               "p50_frame_ms": round(statistics.median(e_ms), 3),
+               "p99_frame_ms": round(float(np.percentile(e_ms, 99)), 3), "components": int(ncomp)}
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel (library profiler, live)
+    hbm, peak_kind = _peaks()
+    kernels = {}
+    for name, (cnt, ms) in prof.items():
+        b = algorithmic_bytes(name, cfg, cnt, S * args.steps) if name in ("recon_a", "recon_b") else \
+            algorithmic_bytes(name, cfg, cnt, S)
+        per_launch_ms = ms / cnt
+        gbs = (b / (per_launch_ms / 1e3) / 1e9) if b else None
+        kernels[name] = {"launches": cnt, "total_ms": round(ms, 3), "share": round(ms / max(total_ms, 1e-9), 4),
+                         "ms_per_launch": round(per_launch_ms, 4),
+                         "achieved_gbs": round(gbs, 1) if gbs else None,
+                         "bytes_per_launch": int(b) if b else None}
+    roofline = None
+    if kernels:
+        dom = max(kernels, key=lambda k: kernels[k]["total_ms"])
+        kd = kernels[dom]
+        traffic = _traffic_from_profiles(dom, args.config)
+        roofline = {"kernel": dom, "bound": "hbm", "achieved": kd["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+                    "frac": round(kd["achieved_gbs"] / hbm, 4) if kd["achieved_gbs"] else None,
+                    "peak_kind": peak_kind, "traffic": traffic, "bytes_per_launch": kd["bytes_per_launch"]}
+
+    # ---- CPU baseline (oracle, all host cores)
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        h1n, h2n = h1.cpu().numpy(), h2.cpu().numpy()
+        t_it, t_slice, t_ccl = cpu_frame_sample(cfg, h1n, h2n, 2 if cfg["gs_iters"] else 0, 16)
+        cpu = {"value": round(cpu_mvoxel_per_s(cfg, t_it, t_slice, t_ccl), 3), "unit": "Mvoxel/s",
+               "cores": len(os.sched_getaffinity(0)), "kind": "port",
+               "sample": f"oracle FP32 (numpy/scipy.fft workers=all): {2 if cfg['gs_iters'] else 0} GS iterations, "
+                         f"16 slices and one labeling at {n}^2, scaled to {cfg['gs_iters']} iterations + {S} slices"}
+
+    line = {
+        "metric": "reconstructed Mvoxel/s + p99 frame latency, chosen vs plain FP32 form, 1 GB300",
+        "value": round(value, 2), "unit": "Mvoxel/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded disc holograms generated on the device)",
+        "config": {"workload": cfg["workload"], "n": n, "slices": S, "dz_um": cfg["dz"], "z0_um": cfg["z0"],
+                   "gs_iterations": cfg["gs_iters"], "discs": cfg["discs"], "form": "fp32-stockham",
+                   "l2": "flushed (512 MiB write) before every timed step",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "p50_frame_ms": round(statistics.median(step_ms), 3),
+        "p99_frame_ms": round(float(np.percentile(step_ms, 99)), 3),
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "kernels": kernels,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def _traffic_from_profiles(kernel: str, config: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any
+    (lines ``traffic <kernel> <config> <bytes_per_launch>`` in profiles/*.md)."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        for line in f.read_text().splitlines():
+            parts = line.strip().strip("`").split()
+            if len(parts) == 4 and parts[0] == "traffic" and parts[1] == kernel and parts[2] == config:
+                try:
+                    return float(parts[3])
+                except ValueError:
+                    pass
+    return None
+
+
+def reference_arm(args, cfg, rank, world):
+    """The reference's CPU path (the oracle port, all host cores) on a bounded
+    sample of the same frame; only rank 0 runs."""
+    if rank != 0:
+        return
+    n = cfg["n"]
+    from oracle import fp64 as o64
+    h1 = o64.synth_hologram(cfg["seed"], min(n, 256), 20, cfg["dmin"], cfg["dmax"], cfg["zmin"], cfg["zmax"])
+    # the sample runs at the full frame size on a tiled stand-in hologram of the same statistics
+    reps = n // h1.shape[0]
+    h1 = np.tile(h1, (reps, reps)).astype(np.float32)
+    h2 = np.roll(h1, 3, axis=1)
+    gs_it = 1 if cfg["gs_iters"] else 0
+    vals = []
+    for i in range(args.warmup + args.steps):
+        t_it, t_slice, t_ccl = cpu_frame_sample(cfg, h1, h2, gs_it, 2)
+        if i >= args.warmup:
+            vals.append(cpu_mvoxel_per_s(cfg, t_it, t_slice, t_ccl))
+    v = float(statistics.mean(vals))
+    frame_ms = cfg["n"] ** 2 * cfg["slices"] / (v * 1e6) * 1e3
+    cores = len(os.sched_getaffinity(0))
+    line = {
+        "metric": "reconstructed Mvoxel/s + p99 frame latency, chosen vs plain FP32 form, 1 GB300",
+        "value": round(v, 3), "unit": "Mvoxel/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(frame_ms, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": cfg["workload"], "n": n, "slices": cfg["slices"], "gs_iterations": cfg["gs_iters"]},
+        "cpu_baseline": {"value": round(v, 3), "unit": "Mvoxel/s", "cores": cores, "kind": "port",
+                         "sample": f"per step: {gs_it} GS iteration(s), 2 slices and one labeling at {n}^2 "
+                                   f"(oracle FP32, scipy.fft workers={cores}), scaled to the full frame"},
+        "e2e": {"value": round(v, 3), "unit": "Mvoxel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

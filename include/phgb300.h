@@ -71,7 +71,8 @@ enum {
 enum {
     PH_OPT_SLICE_BATCH = 1,   /* slices per reconstruction batch (0 = automatic) */
     PH_OPT_USE_GRAPHS = 2,    /* 1 = replay cached CUDA graphs for repeated shapes (default 1) */
-    PH_OPT_LOOP_LIMIT = 3     /* iteration limit of bounded device loops (CCL root chase) */
+    PH_OPT_LOOP_LIMIT = 3,    /* iteration limit of bounded device loops (CCL root chase) */
+    PH_OPT_PROFILE = 4        /* 1 = time every pass kernel with CUDA events (ph_profile_report) */
 };
 
 /* ---- context -------------------------------------------------------------- */
@@ -90,6 +91,11 @@ PH_API size_t ph_scratch_bytes(const ph_ctx *ctx);
 PH_API int32_t ph_reserve(ph_ctx *ctx, int32_t n_fast, int32_t n_slow, int32_t slices, void *stream);
 /* Number of kernels this context has launched since creation. */
 PH_API int64_t ph_kernel_launches(const ph_ctx *ctx);
+/* With PH_OPT_PROFILE on, every pass kernel is bracketed by CUDA events on the
+ * caller's stream.  Writes one line "name,launches,total_ms\n" per kernel
+ * name into buf (NUL-terminated, truncated to cap), then clears the records.
+ * Synchronises on the recorded events.  Returns the bytes needed. */
+PH_API int64_t ph_profile_report(ph_ctx *ctx, char *buf, int64_t cap);
 
 /* ---- transfer functions ---------------------------------------------------- */
 
@@ -188,6 +194,12 @@ PH_API int32_t ph_synth_hologram(ph_ctx *ctx, float *out, int32_t n_fast, int32_
                                  void *stream);
 
 /* ---- connected-component labeling -------------------------------------------- */
+
+/* The thresholding broadcast that feeds the labeling, `img .<= threshold`
+ * (runtests.jl:183, particle_detection usage): out[i] = in[i] <= threshold
+ * as Bool (UInt8 0/1). */
+PH_API int32_t ph_binarize_le(ph_ctx *ctx, uint8_t *out, const float *in, int64_t n, float threshold,
+                              void *stream);
 
 /* cu_connected_component_labeling (ccl.jl:186-211).  `img` (F32 or BOOL) is
  * labelled as a C-row-major rows x cols grid: 8-connected components of equal

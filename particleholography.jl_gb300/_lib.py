@@ -47,6 +47,8 @@ SIGNATURES = {
     "ph_scratch_bytes": (_sz, [_vp]),
     "ph_reserve": (_i32, [_vp, _i32, _i32, _i32, _vp]),
     "ph_kernel_launches": (_i64, [_vp]),
+    "ph_profile_report": (_i64, [_vp, ctypes.c_char_p, _i64]),
+    "ph_binarize_le": (_i32, [_vp, _vp, _vp, _i64, ctypes.c_float, _vp]),
     "ph_transfer_sqrt": (_i32, [_vp, _vp, _i32, _i32, _f64, _f64, _vp]),
     "ph_transfer": (_i32, [_vp, _vp, _vp, _i32, _i32, _f64, _f64, _vp]),
     "ph_transfer_fp64": (_i32, [_vp, _vp, _i32, _i32, _f64, _f64, _f64, _vp]),
@@ -131,6 +133,17 @@ class Context:
 
     def set_option(self, option: int, value: int) -> None:
         raise_for(lib().ph_set_option(self.handle, option, int(value)), self.handle)
+
+    def profile_report(self) -> dict:
+        """{kernel name: (launches, total ms)} of the profiled passes since the last report."""
+        need = int(lib().ph_profile_report(self.handle, None, 0))
+        buf = ctypes.create_string_buffer(max(need, 1))
+        lib().ph_profile_report(self.handle, buf, len(buf))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms = line.split(",")
+            out[name] = (int(cnt), float(ms))
+        return out
 
     @property
     def launches(self) -> int:

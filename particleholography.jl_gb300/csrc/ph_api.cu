@@ -139,6 +139,11 @@ __global__ void k_proj_finish(const unsigned long long *p64, float *proj, int32_
     if (argmin) argmin[i] = (int32_t)(unsigned)(p & 0xffffffffu);
 }
 
+__global__ void k_binarize_le(uint8_t *out, const float *in, size_t n, float thr) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[i] <= thr ? 1 : 0;
+}
+
 __global__ void k_resid_finish(const double *acc, double *out) {
     *out = acc[1] > 0.0 ? sqrt(acc[0] / acc[1]) : 0.0;
 }
@@ -299,6 +304,50 @@ int launched(ph_ctx *ctx, cudaError_t e, const char *what, int count = 1) {
 
 dim3 grid2d(int nx, int ny, dim3 b) { return dim3((nx + b.x - 1) / b.x, (ny + b.y - 1) / b.y); }
 
+// ---------------------------------------------------------------- profiler
+
+cudaEvent_t prof_event(ph_ctx *ctx) {
+    if (!ctx->prof_pool.empty()) {
+        cudaEvent_t e = ctx->prof_pool.back();
+        ctx->prof_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+// Brackets one pass launch with CUDA events on the caller's stream when
+// PH_OPT_PROFILE is on (never inside a stream capture).
+struct ProfScope {
+    ph_ctx *ctx;
+    cudaStream_t s;
+    const char *name;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(ph_ctx *c, cudaStream_t st, const char *n) : ctx(c), s(st), name(n) {
+        if (ctx->opt_profile && !capturing(s)) {
+            a = prof_event(ctx);
+            b = prof_event(ctx);
+            if (a && b) cudaEventRecord(a, s);
+        }
+    }
+    ~ProfScope() {
+        if (a && b) {
+            cudaEventRecord(b, s);
+            ctx->prof.push_back({name, a, b});
+        }
+    }
+};
+
+template <class F>
+int pass(ph_ctx *ctx, cudaStream_t s, const char *name, F &&launch, int count = 1) {
+    ProfScope p(ctx, s, name);
+    return launched(ctx, launch(), name, count);
+}
+
 // ---------------------------------------------------------------- reconstruction plumbing
 
 struct Spectrum {
@@ -325,14 +374,14 @@ int issue_spectrum(ph_ctx *ctx, const float2 *wf, const float2 *hf, const float2
         f.nx_in = nin_x;
         f.ny_in = nin_y;
         f.pad_off = nx / 4;
-        PH_TRY(launched(ctx, launch_fwd_rows(nx, f, s), "forward rows"));
+        PH_TRY(pass(ctx, s, "fwd_rows",[&] { return launch_fwd_rows(nx, f, s); }));
     } else {
         FwdRowsT<FWD_COMPLEX> f{};
         f.src = wf;
         f.dst = a1;
         f.tw = tw_x;
         f.nrows = ny;
-        PH_TRY(launched(ctx, launch_fwd_rows(nx, f, s), "forward rows"));
+        PH_TRY(pass(ctx, s, "fwd_rows",[&] { return launch_fwd_rows(nx, f, s); }));
     }
     SpectrumCols c{};
     c.a1 = a1;
@@ -343,7 +392,7 @@ int issue_spectrum(ph_ctx *ctx, const float2 *wf, const float2 *hf, const float2
     c.nx = nx;
     c.ny = ny;
     c.scale = (float)(1.0 / ((double)nx * (double)ny));
-    PH_TRY(launched(ctx, launch_spectrum(ny, c, s), "spectrum"));
+    PH_TRY(pass(ctx, s, "spectrum", [&] { return launch_spectrum(ny, c, s); }));
     return PH_OK;
 }
 
@@ -412,23 +461,23 @@ int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void 
         a.ny_out = ny_out;
         a.y0 = y0;
         a.k0 = k0;
-        PH_TRY(launched(ctx, launch_recon_a(ny, a, nb, s), "reconstruction pass A"));
+        PH_TRY(pass(ctx, s, "recon_a",[&] { return launch_recon_a(ny, a, nb, s); }));
         if (kind == RK_PROJ) {
             ReconB<EPI_PROJ> b{};
             b.t = t; b.tw = tw_x; b.proj64 = p64; b.rows = ny_out; b.nx_out = nx_out; b.x0 = 0;
             b.k0 = k0; b.nbatch = nb; b.group = group; b.vol_slice_stride = (long long)nx_out * ny_out;
-            PH_TRY(launched(ctx, launch_recon_b(nx, b, s), "reconstruction pass B"));
+            PH_TRY(pass(ctx, s, "recon_b",[&] { return launch_recon_b(nx, b, s); }));
         } else if (kind == RK_CVOL) {
             ReconB<EPI_CVOL> b{};
             b.t = t; b.tw = tw_x; b.vol = vol; b.rows = ny_out; b.nx_out = nx_out; b.x0 = 0;
             b.k0 = k0; b.nbatch = nb; b.group = 1; b.vol_slice_stride = (long long)nx_out * ny_out;
-            PH_TRY(launched(ctx, launch_recon_b(nx, b, s), "reconstruction pass B"));
+            PH_TRY(pass(ctx, s, "recon_b",[&] { return launch_recon_b(nx, b, s); }));
         } else {
             ReconB<EPI_VOL> b{};
             b.t = t; b.tw = tw_x; b.vol = vol; b.vol_dtype = vol_dtype; b.proj64 = want_proj ? p64 : nullptr;
             b.rows = ny_out; b.nx_out = nx_out; b.x0 = x0;
             b.k0 = k0; b.nbatch = nb; b.group = group; b.vol_slice_stride = (long long)nx_out * ny_out;
-            PH_TRY(launched(ctx, launch_recon_b(nx, b, s), "reconstruction pass B"));
+            PH_TRY(pass(ctx, s, "recon_b",[&] { return launch_recon_b(nx, b, s); }));
         }
     }
     if (want_proj) {
@@ -449,7 +498,7 @@ int issue_propagate(ph_ctx *ctx, float2 *out, const float2 *in, const float2 *h,
     f.dst = bufa;
     f.tw = tw_x;
     f.nrows = ny;
-    PH_TRY(launched(ctx, launch_fwd_rows(nx, f, s), "forward rows"));
+    PH_TRY(pass(ctx, s, "fwd_rows",[&] { return launch_fwd_rows(nx, f, s); }));
     GsCol c{};
     c.src = bufa;
     c.h = h;
@@ -458,13 +507,13 @@ int issue_propagate(ph_ctx *ctx, float2 *out, const float2 *in, const float2 *h,
     c.tw = tw_y;
     c.nx = nx;
     c.scale = (float)(1.0 / ((double)nx * (double)ny));
-    PH_TRY(launched(ctx, launch_gs_col(ny, c, s), "column pass"));
+    PH_TRY(pass(ctx, s, "gs_col",[&] { return launch_gs_col(ny, c, s); }));
     GsRow<ROW_INV> r{};
     r.src = bufb;
     r.dst = out;
     r.tw = tw_x;
     r.nrows = ny;
-    PH_TRY(launched(ctx, launch_gs_row(nx, r, s), "inverse rows"));
+    PH_TRY(pass(ctx, s, "inv_rows",[&] { return launch_gs_row(nx, r, s); }));
     return PH_OK;
 }
 
@@ -522,6 +571,11 @@ void ph_destroy(ph_ctx *ctx) {
         DeviceGuard g(ctx->device);
         cudaDeviceSynchronize();
         for (auto &gr : ctx->graphs) cudaGraphExecDestroy(gr.exec);
+        for (auto &r : ctx->prof) {
+            cudaEventDestroy(r.start);
+            cudaEventDestroy(r.stop);
+        }
+        for (auto e : ctx->prof_pool) cudaEventDestroy(e);
         for (auto &kv : ctx->tw) cudaFree(kv.second);
         if (ctx->scratch) cudaFree(ctx->scratch);
         if (ctx->small) cudaFree(ctx->small);
@@ -544,9 +598,45 @@ int32_t ph_set_option(ph_ctx *ctx, int32_t option, int64_t value) {
             if (value < 1) return PH_ERR_INVALID;
             ctx->opt_loop_limit = value;
             return PH_OK;
+        case PH_OPT_PROFILE: ctx->opt_profile = value; return PH_OK;
     }
     set_err(ctx, "unknown option %d", option);
     return PH_ERR_INVALID;
+}
+
+int64_t ph_profile_report(ph_ctx *ctx, char *buf, int64_t cap) {
+    if (ctx == nullptr) return -1;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    DeviceGuard g(ctx->device);
+    std::vector<std::pair<std::string, std::pair<int64_t, double>>> agg;
+    for (auto &r : ctx->prof) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(r.stop) == cudaSuccess && cudaEventElapsedTime(&ms, r.start, r.stop) == cudaSuccess) {
+            auto it = std::find_if(agg.begin(), agg.end(), [&](auto &e) { return e.first == r.name; });
+            if (it == agg.end()) {
+                agg.push_back({r.name, {1, (double)ms}});
+            } else {
+                it->second.first += 1;
+                it->second.second += ms;
+            }
+        }
+        cudaGetLastError();
+        ctx->prof_pool.push_back(r.start);
+        ctx->prof_pool.push_back(r.stop);
+    }
+    ctx->prof.clear();
+    std::string out;
+    char line[256];
+    for (auto &e : agg) {
+        snprintf(line, sizeof line, "%s,%lld,%.6f\n", e.first.c_str(), (long long)e.second.first, e.second.second);
+        out += line;
+    }
+    if (buf && cap > 0) {
+        const size_t n = std::min<size_t>(out.size(), (size_t)cap - 1);
+        memcpy(buf, out.data(), n);
+        buf[n] = '\0';
+    }
+    return (int64_t)out.size() + 1;
 }
 
 size_t ph_scratch_bytes(const ph_ctx *ctx) { return ctx ? ctx->scratch_bytes : 0; }
@@ -671,28 +761,28 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
     f.dst = bufa;
     f.tw = tw_x;
     f.nrows = ny;
-    PH_TRY(launched(ctx, launch_fwd_rows(nx, f, s), "GS first rows"));
+    PH_TRY(pass(ctx, s, "fwd_rows",[&] { return launch_fwd_rows(nx, f, s); }));
     const float scale = (float)(1.0 / ((double)nx * (double)ny));
     for (int it = 0; it < priter; ++it) {
         const bool last = it == priter - 1;
         GsCol c{};
         c.src = bufa; c.h = static_cast<const float2 *>(transfer); c.dst = bufb; c.tw = tw_y; c.nx = nx;
         c.scale = scale;
-        PH_TRY(launched(ctx, launch_gs_col(ny, c, s), "GS column pass"));
+        PH_TRY(pass(ctx, s, "gs_col",[&] { return launch_gs_col(ny, c, s); }));
         GsRow<ROW_MID> r2{};
         r2.src = bufb; r2.holo = holo2; r2.dst = bufa; r2.tw = tw_x; r2.nrows = ny;
         r2.resid = (last && residual) ? acc : nullptr;
-        PH_TRY(launched(ctx, launch_gs_row(nx, r2, s), "GS row pass (plane 2)"));
+        PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return launch_gs_row(nx, r2, s); }));
         c.src = bufa; c.h = static_cast<const float2 *>(invtransfer); c.dst = bufb;
-        PH_TRY(launched(ctx, launch_gs_col(ny, c, s), "GS column pass"));
+        PH_TRY(pass(ctx, s, "gs_col",[&] { return launch_gs_col(ny, c, s); }));
         if (!last) {
             GsRow<ROW_MID> r1{};
             r1.src = bufb; r1.holo = holo1; r1.dst = bufa; r1.tw = tw_x; r1.nrows = ny;
-            PH_TRY(launched(ctx, launch_gs_row(nx, r1, s), "GS row pass (plane 1)"));
+            PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return launch_gs_row(nx, r1, s); }));
         } else {
             GsRow<ROW_FINAL> r1{};
             r1.src = bufb; r1.holo = holo1; r1.dst = o; r1.tw = tw_x; r1.nrows = ny;
-            PH_TRY(launched(ctx, launch_gs_row(nx, r1, s), "GS final row pass"));
+            PH_TRY(pass(ctx, s, "gs_row_final",[&] { return launch_gs_row(nx, r1, s); }));
         }
     }
     if (residual) {
@@ -865,6 +955,20 @@ int32_t ph_reconst_vol_padded(ph_ctx *ctx, uint8_t *vol, float *proj, const void
     PH_LEAVE(ctx);
 }
 
+int32_t ph_binarize_le(ph_ctx *ctx, uint8_t *out, const float *in, int64_t n, float threshold, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(in, "in");
+    if (n < 0) { set_err(ctx, "negative size"); return PH_ERR_SIZE; }
+    if (n > 0) {
+        PH_TRY(pass(ctx, s, "binarize", [&] {
+            k_binarize_le<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, in, (size_t)n, threshold);
+            return cudaGetLastError();
+        }));
+    }
+    PH_LEAVE(ctx);
+}
+
 int32_t ph_ccl(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype, int64_t rows, int64_t cols,
                void *stream) {
     PH_ENTER(ctx, stream);
@@ -880,10 +984,11 @@ int32_t ph_ccl(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype
         return PH_ERR_DTYPE;
     }
     int64_t nl = 0;
-    cudaError_t e = ccl_launch(img, img_dtype == PH_BOOL, labels, rows, cols, ctx->opt_loop_limit,
-                               static_cast<int *>(ctx->small), s, &nl);
+    PH_TRY(pass(ctx, s, "ccl", [&] {
+        return ccl_launch(img, img_dtype == PH_BOOL, labels, rows, cols, ctx->opt_loop_limit,
+                          static_cast<int *>(ctx->small), s, &nl);
+    }, 0));
     ctx->launches += nl;
-    PH_TRY(cuda_status(ctx, e, "labeling"));
     PH_LEAVE(ctx);
 }
 

@@ -9,11 +9,17 @@
 #include <mutex>
 #include <string>
 #include <unordered_map>
+#include <vector>
 
 
 struct ph_graph_entry {
     std::string key;
     cudaGraphExec_t exec = nullptr;
+};
+
+struct ph_prof_record {
+    const char *name;
+    cudaEvent_t start, stop;
 };
 
 struct ph_ctx {
@@ -46,4 +52,9 @@ struct ph_ctx {
     int64_t opt_slice_batch = 0;
     int64_t opt_use_graphs = 1;
     int64_t opt_loop_limit = int64_t(1) << 26;
+    int64_t opt_profile = 0;
+
+    // profiler: pending event pairs and a pool of spare events
+    std::vector<ph_prof_record> prof;
+    std::vector<cudaEvent_t> prof_pool;
 };

@@ -1,0 +1,222 @@
+# ParticleHolographyGB300.jl -- drop-in bodies for ParticleHolography.jl's
+# reconstruction hot path (src/holofunc.jl, src/ccl.jl) that forward to
+# libphgb300.so through `ccall`.  Same exported names, argument types and
+# failure modes (AssertionError / ArgumentError) as the reference.
+#
+# Julia is not available where this library is built, so this file is not
+# exercised by the repository's tests; the same C ABI is exercised from Python
+# (ctypes) by tests/ on a GB300.
+
+module ParticleHolographyGB300
+
+using CUDA
+using FixedPointNumbers
+
+import ParticleHolography: CuTransferSqrtPart, CuTransfer, CuWavefront, CuLowPassFilter
+
+export cu_transfer_sqrt_arr, cu_transfer, cu_gabor_wavefront, cu_phase_retrieval_holo, cu_get_reconst_vol,
+       cu_get_reconst_xyprojection, cu_get_reconst_vol_and_xyprojection, cu_get_reconst_complex_vol,
+       cu_asm_prop!, cu_2d_pad, cu_get_reconst_vol_and_xyprojection_padded,
+       cu_connected_component_labeling, count_labels, cu_find_valid_labels,
+       cu_get_reconst_xyprojection_argmin, cu_apply_low_pass_filter!, cu_apply_low_pass_filter
+
+const libphgb300 = get(ENV, "PHGB300_LIB", joinpath(@__DIR__, "..", "libphgb300.so"))
+
+const PH_OK = Int32(0)
+const PH_ERR_SIZE = Int32(1)
+const PH_ERR_DTYPE = Int32(2)
+const PH_ERR_TOO_LARGE = Int32(3)
+const PH_N0F8, PH_F16, PH_F32, PH_F64, PH_C64, PH_BOOL = Int32.(0:5)
+
+# one context per device, created on first use
+const _ctxs = Dict{Int,Ptr{Cvoid}}()
+function _ctx()
+    dev = CUDA.deviceid(CUDA.device())
+    get!(_ctxs, dev) do
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        st = ccall((:ph_create, libphgb300), Int32, (Int32, Csize_t, Ref{Ptr{Cvoid}}), dev, 0, h)
+        st == PH_OK || error("ph_create failed ($st)")
+        h[]
+    end
+end
+
+_stream() = CUDA.stream().handle
+
+function _check(st::Int32)
+    st == PH_OK && return nothing
+    msg = unsafe_string(ccall((:ph_last_error, libphgb300), Cstring, (Ptr{Cvoid},), _ctx()))
+    st in (PH_ERR_SIZE, PH_ERR_TOO_LARGE) && throw(AssertionError(msg))
+    st == PH_ERR_DTYPE && throw(ArgumentError(msg))
+    error("libphgb300: $msg (status $st)")
+end
+
+const _rt = Dict{Type,Int32}(N0f8 => PH_N0F8, Float16 => PH_F16, Float32 => PH_F32, Float64 => PH_F64)
+_rtcode(T) = haskey(_rt, T) ? _rt[T] :
+    throw(ArgumentError("return_type must be Subtype of AbstractFloat or N0f8. Got $T"))
+
+# ---- holofunc.jl -----------------------------------------------------------------
+
+function cu_transfer_sqrt_arr(datlen::Int, wavlen::AbstractFloat, dx::AbstractFloat)
+    Plane = CuArray{Float32}(undef, datlen, datlen)
+    _check(ccall((:ph_transfer_sqrt, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{Float32}, Int32, Int32, Float64, Float64, Ptr{Cvoid}),
+                 _ctx(), Plane, datlen, datlen, wavlen, dx, _stream()))
+    return CuTransferSqrtPart(Plane)
+end
+
+function cu_transfer(z0::AbstractFloat, datLen::Int, wavLen::AbstractFloat, d_sqr::CuTransferSqrtPart{Float32})
+    Plane = CuArray{ComplexF32}(undef, datLen, datLen)
+    _check(ccall((:ph_transfer, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{Float32}, Int32, Int32, Float64, Float64, Ptr{Cvoid}),
+                 _ctx(), Plane, d_sqr.data, datLen, datLen, z0, wavLen, _stream()))
+    return CuTransfer(Plane)
+end
+
+function cu_gabor_wavefront(holo::CuArray{Float32,2})
+    out = CuArray{ComplexF32}(undef, size(holo))
+    _check(ccall((:ph_gabor_wavefront, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{Float32}, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), out, holo, size(holo, 1), size(holo, 2), _stream()))
+    return CuWavefront(out)
+end
+
+function cu_phase_retrieval_holo(holo1::CuArray{Float32,2}, holo2::CuArray{Float32,2}, transfer::CuTransfer{ComplexF32},
+                                 invtransfer::CuTransfer{ComplexF32}, priter::Int, datlen::Int)
+    @assert size(holo1) == size(holo2) == size(transfer.data) == size(invtransfer.data) == (datlen, datlen) "All arrays must have the same size as ($datlen, $datlen). Got $(size(holo1)), $(size(holo2)), $(size(transfer.data)), $(size(invtransfer.data))."
+    out = CuArray{ComplexF32}(undef, datlen, datlen)
+    _check(ccall((:ph_phase_retrieval, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{Float32}, CuPtr{Float32}, CuPtr{ComplexF32}, CuPtr{ComplexF32},
+                  Int32, Int32, Int32, CuPtr{Float64}, Ptr{Cvoid}),
+                 _ctx(), out, holo1, holo2, transfer.data, invtransfer.data, datlen, datlen, priter, CU_NULL, _stream()))
+    return CuWavefront(out)
+end
+
+function cu_2d_pad(inarr)
+    inlen = size(inarr, 1)
+    out = CuArray{ComplexF32}(undef, 2 * inlen, 2 * inlen)
+    _check(ccall((:ph_pad2d, libphgb300), Int32, (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), out, inarr, inlen, size(inarr, 2), _stream()))
+    return out
+end
+
+function _vol(wavefront, transfer_front, transfer_dz, slices, code, T, proj)
+    @assert size(wavefront.data) == size(transfer_front.data) == size(transfer_dz.data) "All arrays must have the same size. Got $(size(wavefront.data)), $(size(transfer_front.data)), $(size(transfer_dz.data))."
+    vol = CuArray{T}(undef, size(wavefront.data)..., slices)
+    _check(ccall((:ph_reconst_vol, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{Cvoid}, Int32, CuPtr{Float32}, CuPtr{ComplexF32}, CuPtr{ComplexF32},
+                  CuPtr{ComplexF32}, Int32, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), vol, code, proj === nothing ? CU_NULL : proj, wavefront.data, transfer_front.data,
+                 transfer_dz.data, size(wavefront.data, 1), size(wavefront.data, 2), slices, _stream()))
+    return vol
+end
+
+cu_get_reconst_vol(wavefront::CuWavefront{ComplexF32}, transfer_front::CuTransfer{ComplexF32},
+                   transfer_dz::CuTransfer{ComplexF32}, slices::Int, return_type::Type=N0f8) =
+    _vol(wavefront, transfer_front, transfer_dz, slices, _rtcode(return_type), return_type, nothing)
+
+cu_get_reconst_complex_vol(wavefront::CuWavefront{ComplexF32}, transfer_front::CuTransfer{ComplexF32},
+                           transfer_dz::CuTransfer{ComplexF32}, slices::Int) =
+    _vol(wavefront, transfer_front, transfer_dz, slices, PH_C64, ComplexF32, nothing)
+
+function cu_get_reconst_vol_and_xyprojection(wavefront::CuWavefront{ComplexF32}, transfer_front::CuTransfer{ComplexF32},
+                                             transfer_dz::CuTransfer{ComplexF32}, slices::Int, return_type::Type=N0f8)
+    proj = CuArray{Float32}(undef, size(wavefront.data)...)
+    vol = _vol(wavefront, transfer_front, transfer_dz, slices, _rtcode(return_type), return_type, proj)
+    return vol, proj
+end
+
+function _xyproj(wavefront, transfer_front, transfer_dz, slices, argmin)
+    @assert size(wavefront.data) == size(transfer_front.data) == size(transfer_dz.data) "All arrays must have the same size. Got $(size(wavefront.data)), $(size(transfer_front.data)), $(size(transfer_dz.data))."
+    proj = CuArray{Float32}(undef, size(wavefront.data)...)
+    _check(ccall((:ph_reconst_xyproj, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{Float32}, CuPtr{Int32}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CuPtr{ComplexF32},
+                  Int32, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), proj, argmin === nothing ? CU_NULL : argmin, wavefront.data, transfer_front.data,
+                 transfer_dz.data, size(wavefront.data, 1), size(wavefront.data, 2), slices, _stream()))
+    return proj
+end
+
+cu_get_reconst_xyprojection(wavefront::CuWavefront{ComplexF32}, transfer_front::CuTransfer{ComplexF32},
+                            transfer_dz::CuTransfer{ComplexF32}, slices::Int) =
+    _xyproj(wavefront, transfer_front, transfer_dz, slices, nothing)
+
+"New: the projection and the 1-based slice index of its first minimum."
+function cu_get_reconst_xyprojection_argmin(wavefront::CuWavefront{ComplexF32}, transfer_front::CuTransfer{ComplexF32},
+                                            transfer_dz::CuTransfer{ComplexF32}, slices::Int)
+    arg = CuArray{Int32}(undef, size(wavefront.data)...)
+    proj = _xyproj(wavefront, transfer_front, transfer_dz, slices, arg)
+    return proj, arg .+ Int32(1)
+end
+
+function cu_get_reconst_vol_and_xyprojection_padded(wavefront::CuWavefront{ComplexF32}, transfer_front::CuTransfer{ComplexF32},
+                                                    transfer_dz::CuTransfer{ComplexF32}, slices::Int, return_type::Type=N0f8)
+    expected_size = map(x -> 2 * x, size(wavefront.data))
+    @assert expected_size == size(transfer_front.data) == size(transfer_dz.data) "size(transfer_front.data) and size(transfer_dz.data) must be equal to 2*size(wavefront.data). Got $(size(wavefront.data)), $(size(transfer_front.data)), $(size(transfer_dz.data))."
+    datlen = size(wavefront.data, 1)
+    vol = CuArray{N0f8}(undef, datlen, datlen, slices)
+    proj = CuArray{Float32}(undef, datlen, datlen)
+    _check(ccall((:ph_reconst_vol_padded, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{N0f8}, CuPtr{Float32}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CuPtr{ComplexF32},
+                  Int32, Int32, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), vol, proj, wavefront.data, transfer_front.data, transfer_dz.data, datlen,
+                 size(wavefront.data, 2), slices, _rtcode(return_type), _stream()))
+    return vol, proj
+end
+
+function cu_asm_prop!(outholo::CuWavefront, inholo::CuWavefront, d_sqr::CuTransferSqrtPart, zprop::Float64, datlen::Int,
+                      λ::Float64)
+    _check(ccall((:ph_asm_prop, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CuPtr{Float32}, Float64, Int32, Int32, Float64,
+                  Ptr{Cvoid}),
+                 _ctx(), outholo.data, inholo.data, d_sqr.data, zprop, datlen, datlen, λ, _stream()))
+    return nothing
+end
+
+# ---- frequency_filters.jl ---------------------------------------------------------
+
+function cu_apply_low_pass_filter!(holo::CuWavefront, lpf::CuLowPassFilter)
+    _check(ccall((:ph_apply_lpf, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CuPtr{Float32}, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), holo.data, holo.data, lpf.data, size(holo.data, 1), size(holo.data, 2), _stream()))
+    return nothing
+end
+
+function cu_apply_low_pass_filter(holo::CuWavefront, lpf::CuLowPassFilter)
+    out = CuWavefront(copy(holo.data))
+    cu_apply_low_pass_filter!(out, lpf)
+    return out
+end
+
+# ---- ccl.jl ------------------------------------------------------------------------
+
+function cu_connected_component_labeling(input_img)
+    @assert length(input_img) <= 2^32 - 1 "Image is too large. Maximum length is 2^32-1."
+    output_img = CuArray{UInt32}(undef, size(input_img))
+    height, width = size(input_img)
+    code = eltype(input_img) == Bool ? PH_BOOL : PH_F32
+    img = eltype(input_img) in (Bool, Float32) ? input_img : Float32.(input_img)
+    _check(ccall((:ph_ccl, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{UInt32}, CuPtr{Cvoid}, Int32, Int64, Int64, Ptr{Cvoid}),
+                 _ctx(), output_img, img, code, height, width, _stream()))   # the reference's grid: rows = size(img,1)
+    return output_img
+end
+
+function _roots(labels::CuArray{UInt32}, capacity::Int)
+    roots = Vector{Int64}(undef, capacity)
+    count = Ref{Int64}(0)
+    _check(ccall((:ph_ccl_roots, libphgb300), Int32,
+                 (Ptr{Cvoid}, Ptr{Int64}, Int64, Ref{Int64}, CuPtr{UInt32}, Int64, Ptr{Cvoid}),
+                 _ctx(), roots, capacity, count, labels, length(labels), _stream()))
+    return count[], roots
+end
+
+count_labels(labels::CuArray{UInt32}) = _roots(labels, 0)[1]
+count_labels(labels::Array{UInt32}) = count_labels(CuArray(labels))
+
+function cu_find_valid_labels(labels::CuArray{UInt32,2})
+    c, _ = _roots(labels, 0)
+    _, roots = _roots(labels, c)
+    return roots[1:c]
+end
+
+end # module
