@@ -155,6 +155,17 @@ PH_API int32_t ph_propagate(ph_ctx *ctx, void *out, const void *in, const void *
 PH_API int32_t ph_apply_lpf(ph_ctx *ctx, void *out, const void *in, const float *lpf, int32_t n_fast,
                             int32_t n_slow, void *stream);
 
+/* cu_rectangle_filter (frequency_filters.jl:31-38; kernel :5-15): Float32 mask of
+ * size imglen^2, 0 where (x - n/2 + 1)^2 + (y - n/2)^2 >= maxi^2 (x the slow
+ * axis in this library's view, 1-based), else 1. */
+PH_API int32_t ph_lpf_rectangle(ph_ctx *ctx, float *out, int32_t imglen, double prop_dist, double wavlen,
+                                double pitch, void *stream);
+
+/* cu_super_gaussian_filter (frequency_filters.jl:66-74; kernel :40-50):
+ * exp(-1/2 (tx^2 + ty^2)^3), t = (i - n/2 + 1)/n/pitch/sigma, FP64, stored Float32. */
+PH_API int32_t ph_lpf_super_gaussian(ph_ctx *ctx, float *out, int32_t imglen, double prop_dist, double wavlen,
+                                     double pitch, void *stream);
+
 /* cu_get_reconst_xyprojection (holofunc.jl:248-266), plus the argmin depth:
  * proj[y][x] = min_k |ifft(ifftshift(X_k))|^2 (unclamped), X_k =
  * fftshift(fft(wf)).*tf_front.*tf_dz^k; argmin (nullable, int32) = the first k

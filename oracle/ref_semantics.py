@@ -293,6 +293,44 @@ def reconst_vol_and_xyprojection_padded(wf, transfer_front, transfer_dz, slices:
     return vol, xy_projection_from_vol(vol)
 
 
+# ---------------------------------------------------------------- low-pass filters
+
+def _lpf_maxi(prop_dist: float, wavlen: float, imglen: int, pitch: float) -> float:
+    """frequency_filters.jl:33 / :68."""
+    return 1 / wavlen * imglen ** 2 * pitch ** 2 / np.sqrt(4.0 * prop_dist ** 2 + imglen ** 2 * pitch ** 2)
+
+
+def rectangle_filter(prop_dist: float, wavlen: float, imglen: int, pitch: float) -> np.ndarray:
+    """``cu_rectangle_filter`` (frequency_filters.jl:31-38; kernel :5-15).
+
+    ``arr[y, x] = 0`` where ``(x - datlen/2 + 1)^2 + (y - datlen/2)^2 >= maxi^2``
+    (1-based x, y; note the asymmetric offsets), else 1.  ``arr[y, x]`` has y as
+    the fast index, so it is ``a[x-1, y-1]`` here.
+    """
+    maxi = _lpf_maxi(prop_dist, wavlen, imglen, pitch)
+    i = np.arange(1, imglen + 1, dtype=np.float64)
+    xs = (i - imglen / 2 + 1)[:, None]        # x indexes the slow axis (rows of `a`)
+    ys = (i - imglen / 2)[None, :]
+    return np.where(xs ** 2 + ys ** 2 >= maxi ** 2, 0.0, 1.0).astype(np.float32)
+
+
+def super_gaussian_filter(prop_dist: float, wavlen: float, imglen: int, pitch: float) -> np.ndarray:
+    """``cu_super_gaussian_filter`` (frequency_filters.jl:66-74; kernel :40-50), FP64
+    evaluation stored as Float32."""
+    maxi = _lpf_maxi(prop_dist, wavlen, imglen, pitch)
+    sigma = maxi / (imglen * pitch) / (2.0 * np.log(2.0)) ** (1 / 6)
+    i = np.arange(1, imglen + 1, dtype=np.float64)
+    t = (i - imglen / 2 + 1) / imglen / pitch / sigma
+    r2 = (t ** 2)[:, None] + (t ** 2)[None, :]
+    return np.exp(-1 / 2 * r2 ** 3).astype(np.float32)
+
+
+def apply_low_pass_filter(holo: np.ndarray, lpf: np.ndarray) -> np.ndarray:
+    """``cu_apply_low_pass_filter[!]`` (frequency_filters.jl:88-107):
+    ``ifft(ifftshift(lpf .* fftshift(fft(holo))))``."""
+    return _ifft2(ifftshift(np.asarray(lpf, np.float32) * fftshift(_fft2(holo)))).astype(np.complex64)
+
+
 # ---------------------------------------------------------------- labels
 
 def count_labels(labels: np.ndarray) -> int:

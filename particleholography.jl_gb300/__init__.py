@@ -10,6 +10,8 @@ The directory name is not a Python identifier; load the package with
 """
 from . import _lib
 from .ccl import count_labels, cu_connected_component_labeling, cu_find_valid_labels
+from .frequency_filters import (cu_apply_low_pass_filter, cu_apply_low_pass_filter_, cu_rectangle_filter,
+                                cu_super_gaussian_filter)
 from .holofunc import (cu_2d_pad, cu_asm_prop_, cu_gabor_wavefront, cu_get_reconst_complex_vol,
                        cu_get_reconst_vol, cu_get_reconst_vol_and_xyprojection,
                        cu_get_reconst_vol_and_xyprojection_padded, cu_get_reconst_xyprojection,

@@ -60,6 +60,8 @@ SIGNATURES = {
     "ph_reconst_vol": (_i32, [_vp, _vp, _i32, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "ph_reconst_vol_padded": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "ph_propagate": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _vp]),
+    "ph_lpf_rectangle": (_i32, [_vp, _vp, _i32, _f64, _f64, _f64, _vp]),
+    "ph_lpf_super_gaussian": (_i32, [_vp, _vp, _i32, _f64, _f64, _f64, _vp]),
     "ph_apply_lpf": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _vp]),
     "ph_synth_hologram": (_i32, [_vp, _vp, _i32, _i32, _vp, _i32, _f64, _f64, _f64, _vp, _vp]),
     "ph_ccl": (_i32, [_vp, _vp, _vp, _i32, _i64, _i64, _vp]),

@@ -22,6 +22,7 @@ LIB = PKG / "libphgb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 

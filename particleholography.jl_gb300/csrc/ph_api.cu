@@ -144,6 +144,33 @@ __global__ void k_binarize_le(uint8_t *out, const float *in, size_t n, float thr
     if (i < n) out[i] = in[i] <= thr ? 1 : 0;
 }
 
+// frequency_filters.jl:5-15: row i (slow) is the reference's x, column j its y.
+__global__ void k_lpf_rect(float *out, int n, double maxi) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= n || j >= n) return;
+    const double a = (double)(i + 1) - n / 2.0 + 1.0;
+    const double b = (double)(j + 1) - n / 2.0;
+    out[(size_t)i * n + j] = (__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)) >= __dmul_rn(maxi, maxi)) ? 0.0f : 1.0f;
+}
+
+// frequency_filters.jl:40-50.
+__global__ void k_lpf_super_gaussian(float *out, int n, double pitch, double sigma) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= n || j >= n) return;
+    const double tx = ((double)(i + 1) - n / 2.0 + 1.0) / n / pitch / sigma;
+    const double ty = ((double)(j + 1) - n / 2.0 + 1.0) / n / pitch / sigma;
+    const double r2 = tx * tx + ty * ty;
+    out[(size_t)i * n + j] = (float)exp(-0.5 * (r2 * r2 * r2));
+}
+
+// frequency_filters.jl:33: 1/wavlen * imglen^2 * pitch^2 / sqrt(4 d^2 + imglen^2 pitch^2), same order.
+double lpf_maxi(double prop_dist, double wavlen, int imglen, double pitch) {
+    const double n2 = (double)((long long)imglen * imglen), p2 = pitch * pitch;
+    return (1.0 / wavlen) * n2 * p2 / sqrt(4.0 * (prop_dist * prop_dist) + n2 * p2);
+}
+
 __global__ void k_resid_finish(const double *acc, double *out) {
     *out = acc[1] > 0.0 ? sqrt(acc[0] / acc[1]) : 0.0;
 }
@@ -348,6 +375,51 @@ int pass(ph_ctx *ctx, cudaStream_t s, const char *name, F &&launch, int count = 
     return launched(ctx, launch(), name, count);
 }
 
+// ---------------------------------------------------------------- graph replay
+
+// Runs `issue(stream)` (a fixed sequence of launches whose parameters are all
+// captured by `key`) as a cached CUDA graph: recorded once on the context's
+// private capture stream, then launched on `s`.  Profiling, an ongoing capture
+// of `s` by the caller, or PH_OPT_USE_GRAPHS = 0 issue the launches directly.
+template <class F>
+int run_graph(ph_ctx *ctx, cudaStream_t s, const char *key, F &&issue) {
+    if (!ctx->opt_use_graphs || ctx->opt_profile || capturing(s)) return issue(s);
+    for (auto it = ctx->graphs.begin(); it != ctx->graphs.end(); ++it) {
+        if (it->key == key) {
+            ctx->graphs.splice(ctx->graphs.begin(), ctx->graphs, it);
+            PH_CUDA(cudaGraphLaunch(ctx->graphs.front().exec, s), "cudaGraphLaunch");
+            ctx->launches += ctx->graphs.front().kernels;
+            return PH_OK;
+        }
+    }
+    const int64_t l0 = ctx->launches.load();
+    cudaStream_t cs = ctx->capture_stream;
+    PH_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    const int st = issue(cs);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(cs, &g);
+    const int64_t kernels = ctx->launches.load() - l0;
+    ctx->launches = l0;
+    if (st != PH_OK || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        if (st != PH_OK) return st;
+        return cuda_status(ctx, e, "cudaStreamEndCapture");
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return cuda_status(ctx, ei, "cudaGraphInstantiate");
+    ctx->graphs.push_front({key, exec, kernels});
+    while ((int)ctx->graphs.size() > kMaxGraphs) {
+        cudaGraphExecDestroy(ctx->graphs.back().exec);
+        ctx->graphs.pop_back();
+    }
+    PH_CUDA(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
+    ctx->launches += kernels;
+    return PH_OK;
+}
+
 // ---------------------------------------------------------------- reconstruction plumbing
 
 struct Spectrum {
@@ -426,6 +498,11 @@ ReconLayout recon_layout(ph_ctx *ctx, int nx, int ny, int ny_out, int nx_out, in
 
 enum ReconKind { RK_PROJ, RK_VOL, RK_CVOL, RK_PADDED };
 
+int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype, int nx,
+                       int ny, int nx_out, int ny_out, int x0, int y0, int slices, int batch, float4 *state, float2 *t,
+                       unsigned long long *p64, const float2 *tw_x, const float2 *tw_y, bool want_proj,
+                       cudaStream_t s);
+
 // Shared driver of every reconstruction entry point.
 int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype,
                 const float2 *wf, const float2 *hf, const float2 *hdz, int nin_x, int nin_y, int slices,
@@ -445,11 +522,28 @@ int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void 
     float4 *state = at<float4>(ctx, L.state);
     auto *p64 = at<unsigned long long>(ctx, L.p64);
     float2 *t = at<float2>(ctx, L.t);
-    PH_TRY(issue_spectrum(ctx, wf, hf, hdz, nx, ny, padded, nin_x, nin_y, at<float2>(ctx, L.a1), state, tw_x,
-                          tw_y, at<double>(ctx, L.acc), at<float2>(ctx, L.mean), s));
     const bool want_proj = (kind == RK_PROJ) || proj != nullptr || argmin != nullptr;
-    if (want_proj) PH_CUDA(cudaMemsetAsync(p64, 0xff, sizeof(unsigned long long) * nx_out * ny_out, s), "memset");
+    char key[512];
+    snprintf(key, sizeof key, "recon|%d|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%d", (int)kind, nin_x, nin_y, slices,
+             L.batch, vol_dtype, (void *)proj, (void *)argmin, vol, (const void *)wf, (const void *)hf,
+             (const void *)hdz, ctx->scratch, (int)ctx->opt_loop_limit);
+    return run_graph(ctx, s, key, [&](cudaStream_t s) -> int {
+        PH_TRY(issue_spectrum(ctx, wf, hf, hdz, nx, ny, padded, nin_x, nin_y, at<float2>(ctx, L.a1), state, tw_x,
+                              tw_y, at<double>(ctx, L.acc), at<float2>(ctx, L.mean), s));
+        if (want_proj) PH_CUDA(cudaMemsetAsync(p64, 0xff, sizeof(unsigned long long) * nx_out * ny_out, s), "memset");
+        return issue_recon_slices(ctx, kind, proj, argmin, vol, vol_dtype, nx, ny, nx_out, ny_out, x0, y0, slices,
+                                  L.batch, state, t, p64, tw_x, tw_y, want_proj, s);
+    });
+}
 
+// The slice loop of a reconstruction: pass A and pass B per batch, then the
+// projection unpacking.
+int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype, int nx,
+                       int ny, int nx_out, int ny_out, int x0, int y0, int slices, int batch, float4 *state, float2 *t,
+                       unsigned long long *p64, const float2 *tw_x, const float2 *tw_y, bool want_proj,
+                       cudaStream_t s) {
+    ReconLayout L{};
+    L.batch = batch;
     const int group = 8;
     for (int k0 = 0; k0 < slices; k0 += L.batch) {
         const int nb = std::min(L.batch, slices - k0);
@@ -754,6 +848,10 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
     const float2 *tw_x = nullptr, *tw_y = nullptr;
     PH_TRY(get_twiddles(ctx, nx, s, &tw_x));
     PH_TRY(get_twiddles(ctx, ny, s, &tw_y));
+    char key[512];
+    snprintf(key, sizeof key, "gs|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p", nx, ny, priter, out, (const void *)holo1,
+             (const void *)holo2, transfer, invtransfer, (void *)residual, ctx->scratch);
+    PH_TRY(run_graph(ctx, s, key, [&](cudaStream_t s) -> int {
     if (residual) PH_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s), "memset");
 
     FwdRowsT<FWD_SQRT_REAL> f{};
@@ -789,6 +887,8 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
         k_resid_finish<<<1, 1, 0, s>>>(acc, residual);
         PH_TRY(launched(ctx, cudaGetLastError(), "GS residual"));
     }
+    return PH_OK;
+    }));
     PH_LEAVE(ctx);
 }
 
@@ -952,6 +1052,30 @@ int32_t ph_reconst_vol_padded(ph_ctx *ctx, uint8_t *vol, float *proj, const void
     PH_TRY(reconstruct(ctx, RK_PADDED, proj, nullptr, vol, PH_N0F8, static_cast<const float2 *>(wf),
                        static_cast<const float2 *>(tf_front), static_cast<const float2 *>(tf_dz), n_fast, n_slow,
                        slices, s));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_lpf_rectangle(ph_ctx *ctx, float *out, int32_t imglen, double prop_dist, double wavlen, double pitch,
+                         void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    if (imglen <= 0) { set_err(ctx, "imglen must be positive"); return PH_ERR_SIZE; }
+    dim3 b(32, 8);
+    k_lpf_rect<<<grid2d(imglen, imglen, b), b, 0, s>>>(out, imglen, lpf_maxi(prop_dist, wavlen, imglen, pitch));
+    PH_TRY(launched(ctx, cudaGetLastError(), "rectangle filter"));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_lpf_super_gaussian(ph_ctx *ctx, float *out, int32_t imglen, double prop_dist, double wavlen, double pitch,
+                              void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    if (imglen <= 0) { set_err(ctx, "imglen must be positive"); return PH_ERR_SIZE; }
+    const double maxi = lpf_maxi(prop_dist, wavlen, imglen, pitch);
+    const double sigma = maxi / (imglen * pitch) / pow(2.0 * log(2.0), 1.0 / 6.0);
+    dim3 b(32, 8);
+    k_lpf_super_gaussian<<<grid2d(imglen, imglen, b), b, 0, s>>>(out, imglen, pitch, sigma);
+    PH_TRY(launched(ctx, cudaGetLastError(), "super-Gaussian filter"));
     PH_LEAVE(ctx);
 }
 

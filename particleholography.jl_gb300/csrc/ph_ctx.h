@@ -15,6 +15,7 @@
 struct ph_graph_entry {
     std::string key;
     cudaGraphExec_t exec = nullptr;
+    int64_t kernels = 0;   // kernels launched by one replay
 };
 
 struct ph_prof_record {

@@ -47,12 +47,15 @@ struct FftPlan {
 // strided stage writes free of bank conflicts.
 __device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
 
-// Row stride (in float2) of the shared buffer: padded length rounded up to 16,
-// plus 2, so that rows of a CTA fall on different banks when a warp spans rows.
-template <int N>
+// Row stride (in float2) of the shared buffer.  A half-warp of 8-byte accesses
+// covers `rows` rows x `jc` consecutive columns (ROW_FAST: rows fastest; else
+// columns fastest).  Offsetting each row by jc (mod 16) banks puts the rows of a
+// half-warp on disjoint bank pairs.
+template <int N, int ROWS, int P, bool ROW_FAST>
 struct SmemRow {
     static constexpr int PADDED = N + (N >> 4);
-    static constexpr int STRIDE = ((PADDED + 15) / 16) * 16 + 2;
+    static constexpr int JC = ROW_FAST ? 16 / (ROWS < 16 ? ROWS : 16) : (P < 16 ? P : 16);
+    static constexpr int STRIDE = ((PADDED + 15) / 16) * 16 + (JC % 16);
 };
 
 // Twiddle of stage twiddle index i for a length-N transform: W_N^i (forward) or

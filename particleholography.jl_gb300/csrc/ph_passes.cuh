@@ -25,7 +25,10 @@ struct Shape {
     static constexpr int P = N / E;
     static constexpr int ROWS = cmax(1, cmin(64, 512 / P));
     static constexpr int THREADS = ROWS * P;
-    static constexpr int SMEM_BYTES = ROWS * SmemRow<N>::STRIDE * 8;
+    template <bool ROW_FAST>
+    static constexpr int stride() { return SmemRow<N, ROWS, P, ROW_FAST>::STRIDE; }
+    template <bool ROW_FAST>
+    static constexpr int smem_bytes() { return ROWS * stride<ROW_FAST>() * 8; }
 };
 
 template <int N, bool ROW_FAST>
@@ -40,7 +43,7 @@ __global__ void __launch_bounds__(Shape<N>::THREADS) k_pass(const Body body) {
     const int t = threadIdx.x;
     const int r = ThreadMap<N, ROW_FAST>::row(t);
     const int j = ThreadMap<N, ROW_FAST>::j(t);
-    body.template run<N>(ph_smem + r * SmemRow<N>::STRIDE, r, j);
+    body.template run<N>(ph_smem + r * Shape<N>::template stride<ROW_FAST>(), r, j);
 }
 
 __device__ __forceinline__ int shift_idx(int i, int n) {   // centred index of natural frequency i

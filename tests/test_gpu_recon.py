@@ -113,6 +113,26 @@ def test_size_assertions(ph, cuda):
                                                       ph.CuTransfer(to_dev(hdz, cuda)), 2)
 
 
+def test_graph_replay_matches_direct_launches(ph, cuda):
+    """Repeated calls replay a cached CUDA graph; the results equal direct launches."""
+    from ph_gb300 import _lib
+    holo, hf, hdz = _case(256, seed=11)
+    wf = ph.cu_gabor_wavefront(to_dev(holo, cuda))
+    tfs = (ph.CuTransfer(to_dev(hf, cuda)), ph.CuTransfer(to_dev(hdz, cuda)))
+    ctx = _lib.default_context(0)
+    ctx.set_option(_lib.PH_OPT_USE_GRAPHS, 0)
+    p0, a0 = (to_np(t) for t in ph.cu_get_reconst_xyprojection(wf, *tfs, 9, return_argmin=True))
+    ctx.set_option(_lib.PH_OPT_USE_GRAPHS, 1)
+    proj = torch.empty((256, 256), dtype=torch.float32, device=cuda)
+    arg = torch.empty((256, 256), dtype=torch.int32, device=cuda)
+    s = torch.cuda.current_stream().cuda_stream
+    for _ in range(3):
+        proj.zero_()
+        ctx.call("ph_reconst_xyproj", proj.data_ptr(), arg.data_ptr(), wf.data.data_ptr(), tfs[0].data.data_ptr(),
+                 tfs[1].data.data_ptr(), 256, 256, 9, s)
+        assert np.array_equal(to_np(proj), p0) and np.array_equal(to_np(arg), a0)
+
+
 def test_slice_batches_agree(ph, cuda):
     """The result does not depend on how slices are batched between the passes."""
     from ph_gb300 import _lib
