@@ -220,6 +220,21 @@ PH_API int32_t ph_binarize_le(ph_ctx *ctx, uint8_t *out, const float *in, int64_
 PH_API int32_t ph_ccl(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype,
                int64_t rows, int64_t cols, void *stream);
 
+/* The per-slice labeling loop of particle_bounding_boxes (particle_detection.jl:58-76),
+ * in one launch set: `img` holds `slices` images of rows x cols (a binary
+ * volume); each is labelled on its own exactly as ph_ccl labels one image
+ * (labels relative to the image: 1 + the minimum index within the image). */
+PH_API int32_t ph_ccl_batch(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype, int64_t slices,
+                            int64_t rows, int64_t cols, void *stream);
+
+/* get_bounding_rectangles (ccl.jl:240-264) for every component of labels from
+ * ph_ccl / ph_ccl_batch, computed on the device: boxes_host gets up to
+ * `capacity` records of 5 int64 (global 1-based root index, x_min, y_min,
+ * x_max, y_max), x the slow (column) axis and y the fast axis, 1-based, ordered
+ * by root; *count_host = the number of components.  Synchronises. */
+PH_API int32_t ph_ccl_boxes(ph_ctx *ctx, int64_t *boxes_host, int64_t capacity, int64_t *count_host,
+                            const uint32_t *labels, int64_t slices, int64_t rows, int64_t cols, void *stream);
+
 /* count_labels (ccl.jl:213-221) and cu_find_valid_labels (ccl.jl:224-238):
  * writes the sorted 1-based indices i with labels[i] == i into roots_host (up to
  * `capacity` of them, may be NULL when capacity is 0) and their number into

@@ -339,6 +339,18 @@ def count_labels(labels: np.ndarray) -> int:
     return int(np.count_nonzero(flat == np.arange(1, flat.size + 1, dtype=np.int64)))
 
 
+def bounding_rectangles(labels: np.ndarray, valid_labels: np.ndarray) -> list:
+    """``get_bounding_rectangles`` (ccl.jl:240-264) on a Julia ``(height, width)``
+    label array held here as ``(width, height)``: for each valid label,
+    ``(x_min, y_min, x_max, y_max)`` with x the column index j (our slow axis)
+    and y the row index i (our fast axis), 1-based."""
+    out = []
+    for lab in valid_labels:
+        xs, ys = np.nonzero(np.asarray(labels) == lab)     # xs: slow (j - 1), ys: fast (i - 1)
+        out.append((int(xs.min()) + 1, int(ys.min()) + 1, int(xs.max()) + 1, int(ys.max()) + 1))
+    return out
+
+
 def find_valid_labels(labels: np.ndarray) -> np.ndarray:
     """``cu_find_valid_labels`` (ccl.jl:224-238): sorted 1-based linear indices
     ``i`` with ``labels[i] == i`` (the component roots), as Int64."""

@@ -9,7 +9,8 @@ The directory name is not a Python identifier; load the package with
 ``__graft_entry__.load_package()`` (it registers it as ``ph_gb300``).
 """
 from . import _lib
-from .ccl import count_labels, cu_connected_component_labeling, cu_find_valid_labels
+from .ccl import (count_labels, cu_bounding_rectangles, cu_connected_component_labeling,
+                  cu_connected_component_labeling_batch, cu_find_valid_labels)
 from .frequency_filters import (cu_apply_low_pass_filter, cu_apply_low_pass_filter_, cu_rectangle_filter,
                                 cu_super_gaussian_filter)
 from .holofunc import (cu_2d_pad, cu_asm_prop_, cu_gabor_wavefront, cu_get_reconst_complex_vol,

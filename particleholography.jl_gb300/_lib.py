@@ -66,6 +66,8 @@ SIGNATURES = {
     "ph_synth_hologram": (_i32, [_vp, _vp, _i32, _i32, _vp, _i32, _f64, _f64, _f64, _vp, _vp]),
     "ph_ccl": (_i32, [_vp, _vp, _vp, _i32, _i64, _i64, _vp]),
     "ph_ccl_roots": (_i32, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp, _i64, _vp]),
+    "ph_ccl_batch": (_i32, [_vp, _vp, _vp, _i32, _i64, _i64, _i64, _vp]),
+    "ph_ccl_boxes": (_i32, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp, _i64, _i64, _i64, _vp]),
 }
 
 _lib = None

@@ -49,6 +49,49 @@ def cu_connected_component_labeling(input_img: torch.Tensor, reference_grid: boo
     return out.view(torch.uint32) if hasattr(torch, "uint32") else out
 
 
+def cu_connected_component_labeling_batch(vol: torch.Tensor) -> torch.Tensor:
+    """The per-slice labeling of particle_bounding_boxes (particle_detection.jl:58-76)
+    in one launch set: ``vol`` (CUDA Bool/Float32, shape ``(slices, n_slow, n_fast)``)
+    -> UInt32 labels of the same shape, each slice labelled on its own (true 2-D
+    8-connectivity of the slice)."""
+    v = vol.contiguous()
+    if v.dim() != 3 or not v.is_cuda:
+        raise ValueError("expected a 3-D CUDA tensor (slices, n_slow, n_fast)")
+    if v.dtype in (torch.bool, torch.uint8):
+        code, v = _lib.PH_BOOL, v.view(torch.uint8)
+    elif v.dtype == torch.float32:
+        code = _lib.PH_F32
+    else:
+        raise TypeError(f"input must be Float32 or Bool, got {v.dtype}")
+    out = torch.empty(v.shape, dtype=torch.int32, device=v.device)
+    dev = v.device.index if v.device.index is not None else torch.cuda.current_device()
+    _lib.default_context(dev).call("ph_ccl_batch", out.data_ptr(), v.data_ptr(), code, int(v.shape[0]),
+                                   int(v.shape[1]), int(v.shape[2]), torch.cuda.current_stream(dev).cuda_stream)
+    return out.view(torch.uint32) if hasattr(torch, "uint32") else out
+
+
+def cu_bounding_rectangles(labels: torch.Tensor) -> np.ndarray:
+    """get_bounding_rectangles (ccl.jl:240-264) on the device for every component
+    of a label image ``(n_slow, n_fast)`` or label volume ``(slices, n_slow, n_fast)``.
+
+    Returns an int64 array of rows ``(root, x_min, y_min, x_max, y_max)``: the
+    global 1-based root index and the 1-based box, x the slow axis (the
+    reference's column j) and y the fast axis (its row i), ordered by root.
+    """
+    lab = _labels_on_device(labels)
+    shape = tuple(lab.shape)
+    slices, rows, cols = (1,) + shape if len(shape) == 2 else shape
+    dev = lab.device.index if lab.device.index is not None else torch.cuda.current_device()
+    ctx = _lib.default_context(dev)
+    s = torch.cuda.current_stream(dev).cuda_stream
+    count = ctypes.c_int64(0)
+    ctx.call("ph_ccl_boxes", None, 0, ctypes.byref(count), lab.data_ptr(), slices, rows, cols, s)
+    out = np.empty((max(count.value, 1), 5), dtype=np.int64)
+    ctx.call("ph_ccl_boxes", out.ctypes.data, int(count.value), ctypes.byref(count), lab.data_ptr(), slices, rows,
+             cols, s)
+    return out[:count.value]
+
+
 def _labels_on_device(labels) -> torch.Tensor:
     if isinstance(labels, np.ndarray):
         labels = torch.from_numpy(np.ascontiguousarray(labels).view(np.int32)).cuda()

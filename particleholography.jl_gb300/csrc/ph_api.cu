@@ -19,13 +19,15 @@
 #include "ph_launch.cuh"
 
 namespace ph {
-cudaError_t ccl_launch(const void *img, bool is_bool, uint32_t *lab, int64_t rows, int64_t cols, int64_t limit,
-                       int *err, cudaStream_t s, int64_t *launches);
+cudaError_t ccl_launch(const void *img, bool is_bool, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows,
+                       int64_t limit, int *err, cudaStream_t s, int64_t *launches);
 int64_t roots_blocks(int64_t n);
-cudaError_t roots_count_launch(const uint32_t *lab, int64_t n, unsigned *counts, unsigned long long *total,
-                               cudaStream_t s, int64_t *launches);
-cudaError_t roots_write_launch(const uint32_t *lab, int64_t n, const unsigned *offsets, long long *out,
-                               int64_t cap, cudaStream_t s, int64_t *launches);
+cudaError_t roots_count_launch(const uint32_t *lab, int64_t n, int64_t slice_n, unsigned *counts,
+                               unsigned long long *total, cudaStream_t s, int64_t *launches);
+cudaError_t roots_write_launch(const uint32_t *lab, int64_t n, int64_t slice_n, const unsigned *offsets,
+                               long long *out, int64_t cap, unsigned *rank, cudaStream_t s, int64_t *launches);
+cudaError_t boxes_launch(const uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows, const unsigned *rank,
+                         int *boxes, int64_t count, cudaStream_t s, int64_t *launches);
 cudaError_t synth_fill_one(float2 *psi, size_t n, cudaStream_t s);
 cudaError_t synth_disc(float2 *psi, int nx, int ny, double cx, double cy, double diam, double dx, cudaStream_t s);
 cudaError_t synth_finish(const float2 *psi, float *out, size_t n, const float *noise, float *mm, cudaStream_t s);
@@ -1093,9 +1095,8 @@ int32_t ph_binarize_le(ph_ctx *ctx, uint8_t *out, const float *in, int64_t n, fl
     PH_LEAVE(ctx);
 }
 
-int32_t ph_ccl(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype, int64_t rows, int64_t cols,
-               void *stream) {
-    PH_ENTER(ctx, stream);
+static int ccl_common(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype, int64_t rows, int64_t cols,
+                      int64_t slice_rows, cudaStream_t s) {
     PH_NONNULL(labels, "labels");
     PH_NONNULL(img, "img");
     if (rows < 0 || cols < 0) { set_err(ctx, "negative size"); return PH_ERR_SIZE; }
@@ -1109,60 +1110,117 @@ int32_t ph_ccl(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype
     }
     int64_t nl = 0;
     PH_TRY(pass(ctx, s, "ccl", [&] {
-        return ccl_launch(img, img_dtype == PH_BOOL, labels, rows, cols, ctx->opt_loop_limit,
+        return ccl_launch(img, img_dtype == PH_BOOL, labels, rows, cols, slice_rows, ctx->opt_loop_limit,
                           static_cast<int *>(ctx->small), s, &nl);
     }, 0));
     ctx->launches += nl;
+    return PH_OK;
+}
+
+int32_t ph_ccl(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype, int64_t rows, int64_t cols,
+               void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_TRY(ccl_common(ctx, labels, img, img_dtype, rows, cols, rows, s));
     PH_LEAVE(ctx);
 }
 
-int32_t ph_ccl_roots(ph_ctx *ctx, int64_t *roots_host, int64_t capacity, int64_t *count_host, const uint32_t *labels,
-                     int64_t n, void *stream) {
+int32_t ph_ccl_batch(ph_ctx *ctx, uint32_t *labels, const void *img, int32_t img_dtype, int64_t slices, int64_t rows,
+                     int64_t cols, void *stream) {
     PH_ENTER(ctx, stream);
+    if (slices < 0) { set_err(ctx, "negative size"); return PH_ERR_SIZE; }
+    PH_TRY(ccl_common(ctx, labels, img, img_dtype, slices * rows, cols, rows, s));
+    PH_LEAVE(ctx);
+}
+
+// Roots (and optionally their bounding boxes) of labels holding `slices`
+// images of rows x cols; out_host gets `per` int64 per root.  Synchronises.
+static int roots_common(ph_ctx *ctx, const uint32_t *labels, int64_t slices, int64_t rows, int64_t cols, bool boxes,
+                        int64_t *out_host, int64_t capacity, int64_t *count_host, cudaStream_t s) {
     PH_NONNULL(labels, "labels");
     PH_NONNULL(count_host, "count");
-    if (capacity > 0) PH_NONNULL(roots_host, "roots");
-    if (n < 0) { set_err(ctx, "negative size"); return PH_ERR_SIZE; }
+    if (capacity > 0) PH_NONNULL(out_host, "output");
+    if (slices < 0 || rows < 0 || cols < 0) { set_err(ctx, "negative size"); return PH_ERR_SIZE; }
     *count_host = 0;
-    if (n == 0) PH_LEAVE(ctx);
+    const int64_t n = slices * rows * cols, slice_n = rows * cols;
+    if (n == 0) return PH_OK;
     const int64_t nb = roots_blocks(n);
-    Arena a;
-    const size_t oc = a.take<unsigned>(nb);
-    const size_t ot = a.take<unsigned long long>(1);
-    PH_TRY(ensure_scratch(ctx, a.off, s));
     int64_t nl = 0;
-    PH_TRY(cuda_status(ctx, roots_count_launch(labels, n, at<unsigned>(ctx, oc), at<unsigned long long>(ctx, ot), s,
-                                               &nl), "root count"));
+    auto layout = [&](int64_t want, size_t *oc, size_t *ot, size_t *orr, size_t *orank, size_t *obox) {
+        Arena a;
+        *oc = a.take<unsigned>(nb);
+        *ot = a.take<unsigned long long>(1);
+        *orr = a.take<long long>((size_t)std::max<int64_t>(want, 1));
+        *orank = boxes ? a.take<unsigned>((size_t)n) : 0;
+        *obox = boxes ? a.take<int>((size_t)std::max<int64_t>(want, 1) * 4) : 0;
+        return a.off;
+    };
+    size_t oc, ot, orr, orank, obox;
+    PH_TRY(ensure_scratch(ctx, layout(0, &oc, &ot, &orr, &orank, &obox), s));
+    PH_TRY(cuda_status(ctx, roots_count_launch(labels, n, slice_n, at<unsigned>(ctx, oc),
+                                               at<unsigned long long>(ctx, ot), s, &nl), "root count"));
     unsigned long long total = 0;
     int flag = 0;
     PH_CUDA(cudaMemcpyAsync(&total, at<unsigned long long>(ctx, ot), sizeof total, cudaMemcpyDeviceToHost, s),
             "copy count");
     PH_CUDA(cudaMemcpyAsync(&flag, ctx->small, sizeof flag, cudaMemcpyDeviceToHost, s), "copy flag");
     PH_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    ctx->launches += nl;
+    nl = 0;
     if (flag) {
         cudaMemsetAsync(ctx->small, 0, sizeof(int), s);
         set_err(ctx, "a labeling loop reached its iteration limit; labels are incomplete");
-        ctx->launches += nl;
         return PH_ERR_TIMEOUT;
     }
     *count_host = (int64_t)total;
     const int64_t want = std::min<int64_t>((int64_t)total, capacity);
-    if (want > 0) {
-        Arena b = a;
-        const size_t orr = b.take<long long>((size_t)want);
-        // the offsets and total live below `orr`; growing would discard them, so size first
-        if (b.off > ctx->scratch_bytes) {
-            PH_TRY(ensure_scratch(ctx, b.off, s));
-            PH_TRY(cuda_status(ctx, roots_count_launch(labels, n, at<unsigned>(ctx, oc),
-                                                       at<unsigned long long>(ctx, ot), s, &nl), "root count"));
-        }
-        PH_TRY(cuda_status(ctx, roots_write_launch(labels, n, at<unsigned>(ctx, oc), at<long long>(ctx, orr), want, s,
-                                                   &nl), "root write"));
-        PH_CUDA(cudaMemcpyAsync(roots_host, at<long long>(ctx, orr), sizeof(long long) * want, cudaMemcpyDeviceToHost,
+    if (want <= 0) return PH_OK;
+    const size_t need = layout(boxes ? (int64_t)total : want, &oc, &ot, &orr, &orank, &obox);
+    if (need > ctx->scratch_bytes) {   // growing discards the offsets: count again
+        PH_TRY(ensure_scratch(ctx, need, s));
+        PH_TRY(cuda_status(ctx, roots_count_launch(labels, n, slice_n, at<unsigned>(ctx, oc),
+                                                   at<unsigned long long>(ctx, ot), s, &nl), "root count"));
+    }
+    PH_TRY(cuda_status(ctx, roots_write_launch(labels, n, slice_n, at<unsigned>(ctx, oc), at<long long>(ctx, orr),
+                                               want, boxes ? at<unsigned>(ctx, orank) : nullptr, s, &nl),
+                       "root write"));
+    if (!boxes) {
+        PH_CUDA(cudaMemcpyAsync(out_host, at<long long>(ctx, orr), sizeof(long long) * want, cudaMemcpyDeviceToHost,
                                 s), "copy roots");
         PH_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        ctx->launches += nl;
+        return PH_OK;
+    }
+    PH_TRY(cuda_status(ctx, boxes_launch(labels, slices * rows, cols, rows, at<unsigned>(ctx, orank),
+                                         at<int>(ctx, obox), (int64_t)total, s, &nl), "boxes"));
+    std::vector<long long> roots((size_t)want);
+    std::vector<int> bx((size_t)want * 4);
+    PH_CUDA(cudaMemcpyAsync(roots.data(), at<long long>(ctx, orr), sizeof(long long) * want, cudaMemcpyDeviceToHost,
+                            s), "copy roots");
+    PH_CUDA(cudaMemcpyAsync(bx.data(), at<int>(ctx, obox), sizeof(int) * 4 * want, cudaMemcpyDeviceToHost, s),
+            "copy boxes");
+    PH_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    for (int64_t r = 0; r < want; ++r) {   // (root, x_min, y_min, x_max, y_max), 1-based; x = slow axis
+        out_host[5 * r + 0] = roots[r];
+        out_host[5 * r + 1] = bx[4 * r + 0] + 1;
+        out_host[5 * r + 2] = bx[4 * r + 1] + 1;
+        out_host[5 * r + 3] = bx[4 * r + 2] + 1;
+        out_host[5 * r + 4] = bx[4 * r + 3] + 1;
     }
     ctx->launches += nl;
+    return PH_OK;
+}
+
+int32_t ph_ccl_roots(ph_ctx *ctx, int64_t *roots_host, int64_t capacity, int64_t *count_host, const uint32_t *labels,
+                     int64_t n, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_TRY(roots_common(ctx, labels, 1, 1, n, false, roots_host, capacity, count_host, s));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_ccl_boxes(ph_ctx *ctx, int64_t *boxes_host, int64_t capacity, int64_t *count_host, const uint32_t *labels,
+                     int64_t slices, int64_t rows, int64_t cols, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_TRY(roots_common(ctx, labels, slices, rows, cols, true, boxes_host, capacity, count_host, s));
     PH_LEAVE(ctx);
 }
 

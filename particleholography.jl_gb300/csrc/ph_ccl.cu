@@ -70,17 +70,20 @@ __global__ void k_ccl_init(uint32_t *lab, int64_t n) {
     if (i < n) lab[i] = (uint32_t)i;
 }
 
+// One thread per pixel: union with the equal-valued W, NW, N and NE
+// neighbours.  A batch of images is `rows / slice_rows` images stacked along
+// the rows; no union crosses an image boundary.
 template <class T>
-__global__ void k_ccl_union(const T *__restrict__ img, uint32_t *lab, int64_t rows, int64_t cols, int64_t limit,
-                            int *err) {
-    const int64_t x = (int64_t)blockIdx.x * kCclBlockX + threadIdx.x;
-    const int64_t y = (int64_t)blockIdx.y * kCclBlockY + threadIdx.y;
+__global__ void k_ccl_union(const T *__restrict__ img, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows,
+                            int64_t limit, int *err) {
+    const int64_t y = (int64_t)blockIdx.x * kCclBlockY + threadIdx.y;
+    const int64_t x = (int64_t)blockIdx.y * kCclBlockX + threadIdx.x;
     if (x >= cols || y >= rows) return;
     const int64_t i = y * cols + x;
     const T v = img[i];
     if (!ccl_fg<T>(v)) return;
     if (x > 0 && ccl_eq(img[i - 1], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)(i - 1), limit, err);
-    if (y > 0) {
+    if (y % slice_rows != 0) {
         const int64_t u = i - cols;
         if (x > 0 && ccl_eq(img[u - 1], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)(u - 1), limit, err);
         if (ccl_eq(img[u], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)u, limit, err);
@@ -95,34 +98,70 @@ __global__ void k_ccl_compress(const T *__restrict__ img, uint32_t *lab, int64_t
     if (ccl_fg<T>(img[i])) lab[i] = ccl_find_live(lab, (uint32_t)i, limit, err);
 }
 
+// Final labels: 1 + the root's index within its own image, 0 for background.
 template <class T>
-__global__ void k_ccl_background(const T *__restrict__ img, uint32_t *lab, int64_t n) {
+__global__ void k_ccl_background(const T *__restrict__ img, uint32_t *lab, int64_t n, int64_t slice_n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    lab[i] = ccl_fg<T>(img[i]) ? lab[i] + 1u : 0u;
+    const uint32_t base = (uint32_t)((i / slice_n) * slice_n);
+    lab[i] = ccl_fg<T>(img[i]) ? lab[i] - base + 1u : 0u;
 }
 
 template <class T>
-static cudaError_t ccl_run(const T *img, uint32_t *lab, int64_t rows, int64_t cols, int64_t limit, int *err,
-                           cudaStream_t s, int64_t *launches) {
+static cudaError_t ccl_run(const T *img, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows, int64_t limit,
+                           int *err, cudaStream_t s, int64_t *launches) {
     const int64_t n = rows * cols;
     const int tpb = 256;
     const unsigned g1 = (unsigned)((n + tpb - 1) / tpb);
     k_ccl_init<<<g1, tpb, 0, s>>>(lab, n);
     dim3 b2(kCclBlockX, kCclBlockY);
-    dim3 g2((unsigned)((cols + kCclBlockX - 1) / kCclBlockX), (unsigned)((rows + kCclBlockY - 1) / kCclBlockY));
-    k_ccl_union<T><<<g2, b2, 0, s>>>(img, lab, rows, cols, limit, err);
+    dim3 g2((unsigned)((rows + kCclBlockY - 1) / kCclBlockY), (unsigned)((cols + kCclBlockX - 1) / kCclBlockX));
+    k_ccl_union<T><<<g2, b2, 0, s>>>(img, lab, rows, cols, slice_rows, limit, err);
     k_ccl_compress<T><<<g1, tpb, 0, s>>>(img, lab, n, limit, err);
-    k_ccl_background<T><<<g1, tpb, 0, s>>>(img, lab, n);
+    k_ccl_background<T><<<g1, tpb, 0, s>>>(img, lab, n, slice_rows * cols);
     *launches += 4;
     return cudaGetLastError();
 }
 
-cudaError_t ccl_launch(const void *img, bool is_bool, uint32_t *lab, int64_t rows, int64_t cols, int64_t limit,
-                       int *err, cudaStream_t s, int64_t *launches) {
+// Labels `rows x cols` pixels; with slice_rows < rows, every slice_rows rows
+// form an independent image (a batch of slices labelled in one launch set).
+cudaError_t ccl_launch(const void *img, bool is_bool, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows,
+                       int64_t limit, int *err, cudaStream_t s, int64_t *launches) {
     if (rows <= 0 || cols <= 0) return cudaSuccess;
-    if (is_bool) return ccl_run<uint8_t>(static_cast<const uint8_t *>(img), lab, rows, cols, limit, err, s, launches);
-    return ccl_run<float>(static_cast<const float *>(img), lab, rows, cols, limit, err, s, launches);
+    if (slice_rows <= 0 || slice_rows > rows) slice_rows = rows;
+    if (is_bool)
+        return ccl_run<uint8_t>(static_cast<const uint8_t *>(img), lab, rows, cols, slice_rows, limit, err, s,
+                                launches);
+    return ccl_run<float>(static_cast<const float *>(img), lab, rows, cols, slice_rows, limit, err, s, launches);
+}
+
+// ---------------------------------------------------------------- bounding rectangles
+
+// boxes[4 r .. 4 r + 3] = (min slow, min fast, max slow, max fast) over the pixels of root r (0-based).
+__global__ void k_boxes(const uint32_t *__restrict__ lab, int64_t rows, int64_t cols, int64_t slice_rows,
+                        const unsigned *rank, int *boxes) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * cols) return;
+    const uint32_t l = lab[i];
+    if (l == 0) return;
+    const int64_t slice_n = slice_rows * cols;
+    const int64_t base = (i / slice_n) * slice_n;
+    const unsigned r = rank[base + l - 1];
+    const int64_t li = i - base;
+    const int slow = (int)(li / cols), fast = (int)(li % cols);
+    atomicMin(boxes + 4 * r + 0, slow);
+    atomicMin(boxes + 4 * r + 1, fast);
+    atomicMax(boxes + 4 * r + 2, slow);
+    atomicMax(boxes + 4 * r + 3, fast);
+}
+
+__global__ void k_boxes_init(int *boxes, int64_t count) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    boxes[4 * i + 0] = 0x7fffffff;
+    boxes[4 * i + 1] = 0x7fffffff;
+    boxes[4 * i + 2] = -1;
+    boxes[4 * i + 3] = -1;
 }
 
 // ---------------------------------------------------------------- root compaction
@@ -131,16 +170,19 @@ constexpr int kRootThreads = 256;
 constexpr int kRootItems = 16;                       // per thread
 constexpr int kRootTile = kRootThreads * kRootItems; // elements per block
 
-__device__ __forceinline__ bool is_root(const uint32_t *lab, int64_t i) { return lab[i] == (uint32_t)(i + 1); }
+// A root carries its own index (within its image of slice_n pixels) plus one.
+__device__ __forceinline__ bool is_root(const uint32_t *lab, int64_t i, int64_t slice_n) {
+    return lab[i] == (uint32_t)(i % slice_n + 1);
+}
 
-__global__ void k_roots_count(const uint32_t *__restrict__ lab, int64_t n, unsigned *counts) {
+__global__ void k_roots_count(const uint32_t *__restrict__ lab, int64_t n, int64_t slice_n, unsigned *counts) {
     __shared__ unsigned wsum[kRootThreads / 32];
     const int64_t base = (int64_t)blockIdx.x * kRootTile;
     unsigned c = 0;
 #pragma unroll
     for (int k = 0; k < kRootItems; ++k) {
         const int64_t i = base + (int64_t)k * kRootThreads + threadIdx.x;
-        if (i < n && is_root(lab, i)) ++c;
+        if (i < n && is_root(lab, i, slice_n)) ++c;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
@@ -182,9 +224,10 @@ __global__ void k_roots_scan(unsigned *counts, int64_t nb, unsigned long long *t
     if (threadIdx.x == 0) *total = carry;
 }
 
-// Writes the 1-based index of every root, in increasing order.
-__global__ void k_roots_write(const uint32_t *__restrict__ lab, int64_t n, const unsigned *offsets,
-                              long long *out, int64_t cap) {
+// Writes the 1-based linear index of every root, in increasing order, and
+// (rank non-null) rank[i] = the root's position in that order.
+__global__ void k_roots_write(const uint32_t *__restrict__ lab, int64_t n, int64_t slice_n, const unsigned *offsets,
+                              long long *out, int64_t cap, unsigned *rank) {
     __shared__ unsigned wsum[kRootThreads / 32];
     __shared__ unsigned running;
     const int64_t base = (int64_t)blockIdx.x * kRootTile;
@@ -193,14 +236,15 @@ __global__ void k_roots_write(const uint32_t *__restrict__ lab, int64_t n, const
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int k = 0; k < kRootItems; ++k) {
         const int64_t i = base + (int64_t)k * kRootThreads + threadIdx.x;
-        const bool f = i < n && is_root(lab, i);
+        const bool f = i < n && is_root(lab, i, slice_n);
         const unsigned m = __ballot_sync(0xffffffffu, f);
         if (lane == 0) wsum[w] = __popc(m);
         __syncthreads();
         unsigned pre = running;
         for (int q = 0; q < w; ++q) pre += wsum[q];
         pre += __popc(m & ((1u << lane) - 1u));
-        if (f && (int64_t)pre < cap) out[pre] = (long long)(i + 1);
+        if (f && (int64_t)pre < cap && out) out[pre] = (long long)(i + 1);
+        if (f && rank) rank[i] = pre;
         __syncthreads();
         if (threadIdx.x == 0) {
             unsigned t = 0;
@@ -213,20 +257,30 @@ __global__ void k_roots_write(const uint32_t *__restrict__ lab, int64_t n, const
 
 int64_t roots_blocks(int64_t n) { return (n + kRootTile - 1) / kRootTile; }
 
-cudaError_t roots_count_launch(const uint32_t *lab, int64_t n, unsigned *counts, unsigned long long *total,
-                               cudaStream_t s, int64_t *launches) {
+cudaError_t roots_count_launch(const uint32_t *lab, int64_t n, int64_t slice_n, unsigned *counts,
+                               unsigned long long *total, cudaStream_t s, int64_t *launches) {
     const int64_t nb = roots_blocks(n);
-    k_roots_count<<<(unsigned)nb, kRootThreads, 0, s>>>(lab, n, counts);
+    k_roots_count<<<(unsigned)nb, kRootThreads, 0, s>>>(lab, n, slice_n, counts);
     k_roots_scan<<<1, kRootThreads, 0, s>>>(counts, nb, total);
     *launches += 2;
     return cudaGetLastError();
 }
 
-cudaError_t roots_write_launch(const uint32_t *lab, int64_t n, const unsigned *offsets, long long *out,
-                               int64_t cap, cudaStream_t s, int64_t *launches) {
+cudaError_t roots_write_launch(const uint32_t *lab, int64_t n, int64_t slice_n, const unsigned *offsets,
+                               long long *out, int64_t cap, unsigned *rank, cudaStream_t s, int64_t *launches) {
     const int64_t nb = roots_blocks(n);
-    k_roots_write<<<(unsigned)nb, kRootThreads, 0, s>>>(lab, n, offsets, out, cap);
+    k_roots_write<<<(unsigned)nb, kRootThreads, 0, s>>>(lab, n, slice_n, offsets, out, cap, rank);
     *launches += 1;
+    return cudaGetLastError();
+}
+
+// Boxes of `count` roots whose ranks are in `rank` (see k_roots_write).
+cudaError_t boxes_launch(const uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows, const unsigned *rank,
+                         int *boxes, int64_t count, cudaStream_t s, int64_t *launches) {
+    if (count > 0) k_boxes_init<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(boxes, count);
+    const int64_t n = rows * cols;
+    k_boxes<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(lab, rows, cols, slice_rows, rank, boxes);
+    *launches += 2;
     return cudaGetLastError();
 }
 

@@ -94,6 +94,39 @@ def test_loop_limit_reports_timeout(ph, cuda):
     assert ph.count_labels(lab) == 1
 
 
+def test_bounding_rectangles(ph, cuda, golden):
+    g = golden("binaryparticles")
+    img = np.unpackbits(g["fg_bits"])[: int(np.prod(g["shape"]))].reshape(g["shape"]).astype(np.float32)
+    lab_t = ph.cu_connected_component_labeling(to_dev(img, cuda))
+    boxes = ph.cu_bounding_rectangles(lab_t)
+    lab = to_np(lab_t).astype(np.uint32)
+    valid = ref.find_valid_labels(lab)
+    assert boxes.shape == (84, 5) and np.array_equal(boxes[:, 0], valid)
+    want = ref.bounding_rectangles(lab, valid)
+    assert [tuple(b) for b in boxes[:, 1:].tolist()] == want
+
+
+def test_batched_slices_match_per_slice(ph, cuda):
+    """One labeling launch set over a binary volume equals labeling each slice alone."""
+    rng = np.random.default_rng(8)
+    vol = rng.random((6, 96, 80)) < 0.45
+    vol[2] = False                                   # an empty slice
+    lab = to_np(ph.cu_connected_component_labeling_batch(to_dev(vol, cuda))).astype(np.uint32)
+    total = 0
+    for k in range(vol.shape[0]):
+        want = occl.connected_component_labeling(vol[k].astype(np.float32))
+        assert np.array_equal(lab[k], want)
+        total += ref.count_labels(want)
+    boxes = ph.cu_bounding_rectangles(ph.cu_connected_component_labeling_batch(to_dev(vol, cuda)))
+    assert len(boxes) == total
+    n = 96 * 80
+    for root, x0, y0, x1, y1 in boxes[:50]:
+        k, local = divmod(int(root) - 1, n)
+        sl = lab[k]
+        xs, ys = np.nonzero(sl == local + 1)
+        assert (x0, y0, x1, y1) == (xs.min() + 1, ys.min() + 1, xs.max() + 1, ys.max() + 1)
+
+
 def test_deterministic(ph, cuda):
     rng = np.random.default_rng(0)
     img = (rng.random((512, 512)) < 0.55).astype(np.float32)
