@@ -1,13 +1,16 @@
 // ph_ccl.cu -- connected-component labeling of equal-valued 8-connected
 // regions (the semantics of ParticleHolography.jl src/ccl.jl:186-211) by
 // lock-free union-find, plus the root compaction behind count_labels /
-// cu_find_valid_labels (ccl.jl:213-238).
+// cu_find_valid_labels (ccl.jl:213-238) and device-side bounding rectangles.
 //
-// Every label array satisfies L[i] <= i; a union links the larger of two roots
-// to the smaller with atomicMin, so every tree's root is the minimum linear
-// index of its component and the final label (root + 1) matches the
-// reference's.  Chains strictly decrease, so every chase ends; each loop still
-// carries an iteration limit that raises the context's error flag.
+// Union-find after the published ECL-CC scheme (Jaiganesh & Burtscher, HPDC
+// 2018): every parent array satisfies L[i] <= i and i is a root iff L[i] == i;
+// parents start at the smallest equal-valued earlier neighbour; hooking links
+// the larger of two roots to the smaller with compare-and-swap; finds shorten
+// the path they walk (pointer jumping).  The root of a tree is therefore the
+// minimum linear index of its component, and the final label (root + 1) is the
+// reference's.  Every loop is bounded by an iteration limit that raises the
+// context's error flag instead of running on.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -27,47 +30,58 @@ __device__ __forceinline__ bool ccl_fg<uint8_t>(uint8_t v) { return v != 0; }
 __device__ __forceinline__ bool ccl_eq(float a, float b) { return a == b; }
 __device__ __forceinline__ bool ccl_eq(uint8_t a, uint8_t b) { return (a != 0) == (b != 0); }
 
-__device__ __forceinline__ uint32_t ccl_find(const uint32_t *__restrict__ lab, uint32_t x, int64_t limit,
-                                             int *err) {
-    uint32_t p = lab[x];
+// Root of x, shortening the walked path on the way (benign races: every
+// value written is an ancestor of the slot it is written to).
+__device__ __forceinline__ uint32_t ccl_find(uint32_t *lab, uint32_t x, int64_t limit, int *err) {
+    uint32_t cur = __ldcg(lab + x);
+    if (cur == x) return x;
+    uint32_t prev = x;
     int64_t it = 0;
-    while (p != x) {
-        x = p;
-        p = lab[x];
+    uint32_t next;
+    while (cur > (next = __ldcg(lab + cur))) {
+        lab[prev] = next;
+        prev = cur;
+        cur = next;
         if (++it > limit) { atomicExch(err, 1); break; }
     }
-    return x;
+    return cur;
 }
 
-// Volatile-free find for the union phase: labels change under us, so re-read.
-__device__ __forceinline__ uint32_t ccl_find_live(uint32_t *lab, uint32_t x, int64_t limit, int *err) {
-    uint32_t p = __ldcg(lab + x);
+// Links the trees of a and b (the larger root under the smaller).
+__device__ __forceinline__ void ccl_hook(uint32_t *lab, uint32_t a, uint32_t b, int64_t limit, int *err) {
+    uint32_t ra = ccl_find(lab, a, limit, err);
+    uint32_t rb = ccl_find(lab, b, limit, err);
     int64_t it = 0;
-    while (p != x) {
-        x = p;
-        p = __ldcg(lab + x);
-        if (++it > limit) { atomicExch(err, 1); break; }
-    }
-    return x;
-}
-
-__device__ __forceinline__ void ccl_unite(uint32_t *lab, uint32_t a, uint32_t b, int64_t limit, int *err) {
-    int64_t it = 0;
-    while (true) {
-        a = ccl_find_live(lab, a, limit, err);
-        b = ccl_find_live(lab, b, limit, err);
-        if (a == b) return;
-        if (a < b) { uint32_t t = a; a = b; b = t; }
-        const uint32_t old = atomicMin(lab + a, b);
-        if (old == a) return;
-        a = old;
+    while (ra != rb) {
+        if (ra < rb) { uint32_t t = ra; ra = rb; rb = t; }
+        // ra > rb: make ra point to rb if ra is still a root
+        const uint32_t ret = atomicCAS(lab + ra, ra, rb);
+        if (ret == ra) return;
+        ra = ret;   // ra gained a parent meanwhile: continue from it
         if (++it > limit) { atomicExch(err, 1); return; }
     }
 }
 
-__global__ void k_ccl_init(uint32_t *lab, int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) lab[i] = (uint32_t)i;
+// Initial parents: the smallest equal-valued earlier neighbour (NW < N < NE < W
+// in linear order), else the pixel itself.
+template <class T>
+__global__ void k_ccl_init(const T *__restrict__ img, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows) {
+    const int64_t y = (int64_t)blockIdx.x * kCclBlockY + threadIdx.y;
+    const int64_t x = (int64_t)blockIdx.y * kCclBlockX + threadIdx.x;
+    if (x >= cols || y >= rows) return;
+    const int64_t i = y * cols + x;
+    const T v = img[i];
+    int64_t p = i;
+    if (ccl_fg<T>(v)) {
+        if (x > 0 && ccl_eq(img[i - 1], v)) p = i - 1;
+        if (y % slice_rows != 0) {
+            const int64_t u = i - cols;
+            if (x + 1 < cols && ccl_eq(img[u + 1], v)) p = u + 1;
+            if (ccl_eq(img[u], v)) p = u;
+            if (x > 0 && ccl_eq(img[u - 1], v)) p = u - 1;
+        }
+    }
+    lab[i] = (uint32_t)p;
 }
 
 // One thread per pixel: union with the equal-valued W, NW, N and NE
@@ -82,12 +96,12 @@ __global__ void k_ccl_union(const T *__restrict__ img, uint32_t *lab, int64_t ro
     const int64_t i = y * cols + x;
     const T v = img[i];
     if (!ccl_fg<T>(v)) return;
-    if (x > 0 && ccl_eq(img[i - 1], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)(i - 1), limit, err);
+    if (x > 0 && ccl_eq(img[i - 1], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)(i - 1), limit, err);
     if (y % slice_rows != 0) {
         const int64_t u = i - cols;
-        if (x > 0 && ccl_eq(img[u - 1], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)(u - 1), limit, err);
-        if (ccl_eq(img[u], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)u, limit, err);
-        if (x + 1 < cols && ccl_eq(img[u + 1], v)) ccl_unite(lab, (uint32_t)i, (uint32_t)(u + 1), limit, err);
+        if (x > 0 && ccl_eq(img[u - 1], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)(u - 1), limit, err);
+        if (ccl_eq(img[u], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)u, limit, err);
+        if (x + 1 < cols && ccl_eq(img[u + 1], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)(u + 1), limit, err);
     }
 }
 
@@ -95,7 +109,7 @@ template <class T>
 __global__ void k_ccl_compress(const T *__restrict__ img, uint32_t *lab, int64_t n, int64_t limit, int *err) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (ccl_fg<T>(img[i])) lab[i] = ccl_find_live(lab, (uint32_t)i, limit, err);
+    if (ccl_fg<T>(img[i])) lab[i] = ccl_find(lab, (uint32_t)i, limit, err);
 }
 
 // Final labels: 1 + the root's index within its own image, 0 for background.
@@ -113,9 +127,9 @@ static cudaError_t ccl_run(const T *img, uint32_t *lab, int64_t rows, int64_t co
     const int64_t n = rows * cols;
     const int tpb = 256;
     const unsigned g1 = (unsigned)((n + tpb - 1) / tpb);
-    k_ccl_init<<<g1, tpb, 0, s>>>(lab, n);
     dim3 b2(kCclBlockX, kCclBlockY);
     dim3 g2((unsigned)((rows + kCclBlockY - 1) / kCclBlockY), (unsigned)((cols + kCclBlockX - 1) / kCclBlockX));
+    k_ccl_init<T><<<g2, b2, 0, s>>>(img, lab, rows, cols, slice_rows);
     k_ccl_union<T><<<g2, b2, 0, s>>>(img, lab, rows, cols, slice_rows, limit, err);
     k_ccl_compress<T><<<g1, tpb, 0, s>>>(img, lab, n, limit, err);
     k_ccl_background<T><<<g1, tpb, 0, s>>>(img, lab, n, slice_rows * cols);

@@ -52,7 +52,7 @@ struct ph_ctx {
 
     int64_t opt_slice_batch = 0;
     int64_t opt_use_graphs = 1;
-    int64_t opt_loop_limit = int64_t(1) << 26;
+    int64_t opt_loop_limit = int64_t(1) << 20;
     int64_t opt_profile = 0;
 
     // profiler: pending event pairs and a pool of spare events

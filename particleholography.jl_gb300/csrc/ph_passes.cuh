@@ -168,7 +168,8 @@ struct ReconA {
             },
             [&](int, int y, float2 v) {
                 const int yo = y - y0;
-                if (valid && yo >= 0 && yo < ny_out) tb[(size_t)yo * nx + kx] = v;
+                // streaming store: T passes through L2 once; keep the state resident instead
+                if (valid && yo >= 0 && yo < ny_out) __stcs(tb + (size_t)yo * nx + kx, v);
             });
     }
 };
@@ -217,7 +218,7 @@ struct ReconB {
             const float2 *tb = t + ((size_t)b * rows + (valid ? y : 0)) * N;
             fft_row<N, E, true>(
                 srow, j, tw,
-                [&](int, int kx) -> float2 { return valid ? tb[kx] : make_float2(0.f, 0.f); },
+                [&](int, int kx) -> float2 { return valid ? __ldcs(tb + kx) : make_float2(0.f, 0.f); },
                 [&](int slot, int x, float2 v) {
                     if constexpr (EPI == EPI_PROJ) {
                         const float in = fmaf(v.x, v.x, v.y * v.y);

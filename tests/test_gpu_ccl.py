@@ -89,7 +89,7 @@ def test_loop_limit_reports_timeout(ph, cuda):
         with pytest.raises(_lib.PhError, match="iteration limit"):
             ph.count_labels(lab)
     finally:
-        ctx.set_option(_lib.PH_OPT_LOOP_LIMIT, 1 << 26)
+        ctx.set_option(_lib.PH_OPT_LOOP_LIMIT, 1 << 20)
     lab = ph.cu_connected_component_labeling(to_dev(img, cuda))
     assert ph.count_labels(lab) == 1
 
