@@ -6,6 +6,7 @@
 
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -617,7 +618,15 @@ int issue_propagate(ph_ctx *ctx, float2 *out, const float2 *in, const float2 *h,
 
 // ====================================================================== C ABI
 
+// An NVTX range named after the entry point spans every call (visible in
+// Nsight timelines; a no-op without a tool attached).
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
 #define PH_ENTER(ctx, stream)                             \
+    NvtxRange _nvtx(__func__);                            \
     if ((ctx) == nullptr) return PH_ERR_INVALID;          \
     std::lock_guard<std::mutex> _lk((ctx)->mu);           \
     DeviceGuard _dg((ctx)->device);                       \
