@@ -23,7 +23,7 @@
  *    HBM budget given at creation), twiddle tables and cached CUDA graphs.
  *    Calls on one context are serialised: a call issued on a different stream
  *    than the previous call first waits for the previous call's work.
- *  - FFT lengths: every power of two from 1 to 8192 per axis (n_fast and
+ *  - FFT lengths: 2^a up to 8192 and 3*2^a up to 6144, per axis (n_fast and
  *    n_slow independently).  Other lengths return PH_ERR_UNSUPPORTED.
  */
 #ifndef PHGB300_H

@@ -321,7 +321,9 @@ int check_len(ph_ctx *ctx, int nx, int ny) {
         return PH_ERR_SIZE;
     }
     if (!supported_len(nx) || !supported_len(ny)) {
-        set_err(ctx, "FFT length (%d, %d) is not supported: each axis must be a power of two up to 8192.", nx, ny);
+        set_err(ctx,
+                "FFT length (%d, %d) is not supported: each axis must be 2^a up to 8192 or 3*2^a up to 6144.", nx,
+                ny);
         return PH_ERR_UNSUPPORTED;
     }
     return PH_OK;

@@ -127,6 +127,18 @@ __device__ __forceinline__ void dft4(float2 &a0, float2 &a1, float2 &a2, float2 
     a3 = csub(d02, r);
 }
 
+// Radix 3: X1,2 = a - (b + c)/2 -/+ i (sqrt(3)/2)(b - c) (forward; signs swap for inverse).
+template <bool INV>
+__device__ __forceinline__ void dft3(float2 &a, float2 &b, float2 &c) {
+    constexpr float h = 0.86602540378443864676f;   // sqrt(3)/2
+    const float2 s = cadd(b, c), d = csub(b, c);
+    const float2 m = make_float2(fmaf(-0.5f, s.x, a.x), fmaf(-0.5f, s.y, a.y));
+    const float2 r = INV ? make_float2(-h * d.y, h * d.x) : make_float2(h * d.y, -h * d.x);   // (+/-) i h d
+    a = cadd(a, s);
+    b = cadd(m, r);
+    c = csub(m, r);
+}
+
 template <int R, bool INV>
 __device__ __forceinline__ void dft(float2 (&v)[R]);
 
@@ -167,6 +179,8 @@ __device__ __forceinline__ void dft(float2 (&v)[R]) {
     if constexpr (R == 1) {
     } else if constexpr (R == 2) {
         dft2<INV>(v[0], v[1]);
+    } else if constexpr (R == 3) {
+        dft3<INV>(v[0], v[1], v[2]);
     } else if constexpr (R == 4) {
         dft4<INV>(v[0], v[1], v[2], v[3]);
     } else if constexpr (R == 8) {

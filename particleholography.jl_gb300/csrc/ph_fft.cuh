@@ -23,22 +23,32 @@
 
 namespace ph {
 
+// Radix plan of a length-N transform with E values per thread.  N is a power
+// of two (radix-E stages, then a smaller power-of-two radix) or three times a
+// power of two (E = 3 E2: radix-E2 stages, a smaller power-of-two radix, and a
+// final radix-3 stage, so every stage before the last has a power-of-two
+// span).  Every radix divides E.
 template <int N, int E>
 struct FftPlan {
-    static_assert((N & (N - 1)) == 0 && N >= 1, "N must be a power of two");
-    static_assert((E & (E - 1)) == 0 && E >= 1 && E <= N, "E must be a power of two <= N");
+    static constexpr bool POW2 = (N & (N - 1)) == 0;
+    static_assert(N >= 1 && (POW2 || ((N % 3) == 0 && ((N / 3) & (N / 3 - 1)) == 0)), "N must be 2^a or 3*2^a");
+    static_assert(E >= 1 && E <= N && N % E == 0, "E must divide N");
     static constexpr int P = N / E;                       // threads per row
-    static constexpr int LOGN = ilog2c(N);
-    static constexpr int LOGE = ilog2c(E);
+    static constexpr int NP2 = POW2 ? N : N / 3;          // power-of-two part of N
+    static constexpr int R2 = POW2 ? E : E / 3;           // main power-of-two radix
+    static constexpr int LOGN = ilog2c(NP2);
+    static constexpr int LOGE = ilog2c(R2);
     static constexpr int NFULL = LOGE == 0 ? 0 : LOGN / LOGE;
-    static constexpr int LAST = 1 << (LOGN - NFULL * LOGE);   // trailing radix (1 = none)
-    static constexpr int NSTAGES = NFULL + (LAST > 1 ? 1 : 0);
+    static constexpr int LAST = 1 << (LOGN - NFULL * LOGE);   // trailing power-of-two radix (1 = none)
+    static constexpr int NSTAGES = NFULL + (LAST > 1 ? 1 : 0) + (POW2 ? 0 : 1);
     template <int S>
-    __host__ __device__ static constexpr int radix() { return S < NFULL ? E : LAST; }
+    __host__ __device__ static constexpr int radix() {
+        return S < NFULL ? R2 : ((LAST > 1 && S == NFULL) ? LAST : 3);
+    }
     template <int S>
     __host__ __device__ static constexpr int ns() {   // product of the radices before stage S
         int v = 1;
-        for (int t = 0; t < S; ++t) v *= (t < NFULL ? E : LAST);
+        for (int t = 0; t < S; ++t) v *= (t < NFULL ? R2 : ((LAST > 1 && t == NFULL) ? LAST : 3));
         return v;
     }
 };

@@ -6,12 +6,15 @@
 
 namespace ph {
 
-// Every supported transform length (powers of two, 1..8192).
-#define PH_FOR_EACH_N(X) \
-    X(1) X(2) X(4) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(8192)
+// Every supported transform length: 2^a (1..8192) and 3 * 2^a (3..6144).
+#define PH_FOR_EACH_N(X)                                                                                  \
+    X(1) X(2) X(4) X(8) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(8192) X(3) X(6) \
+        X(12) X(24) X(48) X(96) X(192) X(384) X(768) X(1536) X(3072) X(6144)
 
 inline bool supported_len(int n) {
-    return n >= 1 && n <= 8192 && (n & (n - 1)) == 0;
+    if (n < 1) return false;
+    if ((n & (n - 1)) == 0) return n <= 8192;
+    return n % 3 == 0 && ((n / 3) & (n / 3 - 1)) == 0 && n <= 6144;
 }
 
 // Rows per CTA of the pass compiled for length n.

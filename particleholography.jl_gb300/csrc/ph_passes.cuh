@@ -21,7 +21,8 @@ namespace ph {
 
 template <int N>
 struct Shape {
-    static constexpr int E = N < 16 ? N : 16;
+    static constexpr bool POW2 = (N & (N - 1)) == 0;
+    static constexpr int E = POW2 ? (N < 16 ? N : 16) : (N < 24 ? N : 24);
     static constexpr int P = N / E;
     static constexpr int ROWS = cmax(1, cmin(64, 512 / P));
     static constexpr int THREADS = ROWS * P;

@@ -41,7 +41,8 @@ def test_xyprojection_golden(ph, cuda, golden):
     assert np.mean(to_np(arg) == g["rec_argmin"]) >= ARGMIN_AGREE
 
 
-@pytest.mark.parametrize("nx,ny", [(32, 16), (16, 64), (256, 128)])
+@pytest.mark.parametrize("nx,ny", [(32, 16), (16, 64), (256, 128), (3, 6), (12, 24), (96, 48), (768, 384),
+                                   (2048, 1536), (1536, 1536)])
 def test_rectangular_projection(ph, cuda, nx, ny):
     holo, hf, hdz = _case(nx, seed=3, n_slow=ny)
     wf = ph.cu_gabor_wavefront(to_dev(holo, cuda))

@@ -98,7 +98,7 @@ def test_gs_golden(ph, cuda, golden):
     assert abs(float(res) - float(g["gs_resid"])) < 1e-4 * max(1.0, float(g["gs_resid"]))
 
 
-@pytest.mark.parametrize("n,iters", [(1, 2), (8, 3), (128, 4), (512, 3)])
+@pytest.mark.parametrize("n,iters", [(1, 2), (8, 3), (128, 4), (512, 3), (96, 3), (768, 2)])
 def test_gs_matches_oracle(ph, cuda, n, iters):
     rng = np.random.default_rng(n)
     h1 = rng.uniform(0.1, 1.0, (n, n)).astype(np.float32)
