@@ -1,4 +1,4 @@
-// Forward row passes and the spectrum-state column pass.
+// Forward row passes (transposed store).
 #include "ph_launch.cuh"
 
 namespace ph {
@@ -11,9 +11,6 @@ cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_SQRT_REAL> &b, cudaStream_
 }
 cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_PADDED> &b, cudaStream_t s) {
     return launch_len<true>(n, b, b.nrows, 1, s);
-}
-cudaError_t launch_spectrum(int n, const SpectrumCols &b, cudaStream_t s) {
-    return launch_len<true>(n, b, b.nx, 1, s);
 }
 
 }  // namespace ph

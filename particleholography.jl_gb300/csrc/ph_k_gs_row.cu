@@ -1,4 +1,4 @@
-// Gerchberg-Saxton / propagation passes.
+// Gerchberg-Saxton / propagation row passes.
 #include "ph_launch.cuh"
 
 namespace ph {
@@ -11,9 +11,6 @@ cudaError_t launch_gs_row(int n, const GsRow<ROW_FINAL> &b, cudaStream_t s) {
 }
 cudaError_t launch_gs_row(int n, const GsRow<ROW_INV> &b, cudaStream_t s) {
     return launch_len<false>(n, b, b.nrows, 1, s);
-}
-cudaError_t launch_gs_col(int n, const GsCol &b, cudaStream_t s) {
-    return launch_len<true>(n, b, b.nx, 1, s);
 }
 
 }  // namespace ph
