@@ -71,7 +71,8 @@ SIGNATURES = {
 }
 
 _lib = None
-_lock = threading.Lock()
+_lock = threading.Lock()            # guards loading the library
+_ctx_lock = threading.Lock()        # guards the per-device context table
 
 
 class PhError(RuntimeError):
@@ -165,7 +166,8 @@ def default_context(device: int) -> Context:
     """The process-wide context of a device (created on first use)."""
     ctx = _contexts.get(device)
     if ctx is None:
-        with _lock:
+        lib()                       # load outside the table lock
+        with _ctx_lock:
             ctx = _contexts.get(device)
             if ctx is None:
                 ctx = _contexts[device] = Context(device)
