@@ -63,6 +63,17 @@ def test_create_without_gpu_fails_cleanly(ph):
     assert not h.value
 
 
+@pytest.mark.timeout(60)
+def test_default_context_without_gpu_raises(ph):
+    """The first context creation loads the library and fails cleanly (no deadlock) without a GPU."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from ph_gb300 import _lib
+    with pytest.raises(_lib.PhError, match="ph_create"):
+        _lib.default_context(0)
+
+
 def test_host_mirror_validates_before_launch(ph):
     """Size and dtype checks happen on the host with the reference's messages."""
     import torch
