@@ -47,6 +47,19 @@ __device__ __forceinline__ uint32_t ccl_find(uint32_t *lab, uint32_t x, int64_t 
     return cur;
 }
 
+// Root of x without writing anything: the flatten pass may not shorten other
+// pixels' paths, or a shortcut written after that pixel's own final root would
+// leave a non-root label behind.
+__device__ __forceinline__ uint32_t ccl_root(const uint32_t *lab, uint32_t x, int64_t limit, int *err) {
+    uint32_t cur = __ldcg(lab + x), next;
+    int64_t it = 0;
+    while (cur > (next = __ldcg(lab + cur))) {
+        cur = next;
+        if (++it > limit) { atomicExch(err, 1); break; }
+    }
+    return cur;
+}
+
 // Links the trees of a and b (the larger root under the smaller).
 __device__ __forceinline__ void ccl_hook(uint32_t *lab, uint32_t a, uint32_t b, int64_t limit, int *err) {
     uint32_t ra = ccl_find(lab, a, limit, err);
@@ -109,7 +122,7 @@ template <class T>
 __global__ void k_ccl_compress(const T *__restrict__ img, uint32_t *lab, int64_t n, int64_t limit, int *err) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (ccl_fg<T>(img[i])) lab[i] = ccl_find(lab, (uint32_t)i, limit, err);
+    if (ccl_fg<T>(img[i])) lab[i] = ccl_root(lab, (uint32_t)i, limit, err);
 }
 
 // Final labels: 1 + the root's index within its own image, 0 for background.
