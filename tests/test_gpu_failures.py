@@ -36,8 +36,8 @@ def test_argument_errors(ph, cuda):
     s = torch.cuda.current_stream().cuda_stream
     x = torch.ones((12, 12), dtype=torch.complex64, device=cuda)
     p = torch.empty((12, 12), dtype=torch.float32, device=cuda)
-    with pytest.raises(_lib.PhError, match="not supported"):          # 12 is not a power of two
-        ctx.call("ph_reconst_xyproj", p.data_ptr(), None, x.data_ptr(), x.data_ptr(), x.data_ptr(), 12, 12, 2, s)
+    with pytest.raises(_lib.PhError, match="not supported"):          # 10 is neither 2^a nor 3*2^a
+        ctx.call("ph_reconst_xyproj", p.data_ptr(), None, x.data_ptr(), x.data_ptr(), x.data_ptr(), 10, 10, 2, s)
     with pytest.raises(_lib.PhError, match="must not be NULL"):
         ctx.call("ph_reconst_xyproj", p.data_ptr(), None, None, x.data_ptr(), x.data_ptr(), 8, 8, 2, s)
     with pytest.raises(AssertionError, match="slices must be >= 1"):
