@@ -30,6 +30,7 @@ PH_N0F8, PH_F16, PH_F32, PH_F64, PH_C64, PH_BOOL = range(6)
 PH_OPT_SLICE_BATCH = 1
 PH_OPT_USE_GRAPHS = 2
 PH_OPT_LOOP_LIMIT = 3
+PH_OPT_PROFILE = 4
 
 _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
@@ -141,9 +142,11 @@ class Context:
 
     def profile_report(self) -> dict:
         """{kernel name: (launches, total ms)} of the profiled passes since the last report."""
-        need = int(lib().ph_profile_report(self.handle, None, 0))
-        buf = ctypes.create_string_buffer(max(need, 1))
-        lib().ph_profile_report(self.handle, buf, len(buf))
+        # one call: the report also clears the records
+        buf = ctypes.create_string_buffer(1 << 16)
+        need = int(lib().ph_profile_report(self.handle, buf, len(buf)))
+        if need > len(buf):
+            raise PhError(PH_ERR_INVALID, f"profile report truncated ({need} bytes)")
         out = {}
         for line in buf.value.decode().splitlines():
             name, cnt, ms = line.split(",")
