@@ -179,7 +179,7 @@ def normalise_with_noise(intensity: np.ndarray, seed: int, sigma: float) -> np.n
     lo, hi = float(intensity.min()), float(intensity.max())
     scale = 1.0 / (hi - lo) if hi > lo else 0.0
     out = (intensity - lo) * scale + noise(seed, intensity.shape, sigma)
-    return out.astype(np.float32)
+    return np.maximum(out, 0.0).astype(np.float32)      # a sensor records no negative intensity
 
 
 def synth_hologram(seed: int, n: int, count: int, dmin: float, dmax: float, zmin: float, zmax: float,

@@ -57,7 +57,7 @@ __global__ void k_normalise_noise(float *out, const float *noise, size_t n, cons
     const float lo = mm[0], hi = mm[1];
     const float scale = hi > lo ? 1.0f / (hi - lo) : 0.0f;
     float v = (out[i] - lo) * scale;
-    if (noise) v += noise[i];
+    if (noise) v = fmaxf(v + noise[i], 0.0f);   // a sensor records no negative intensity
     out[i] = v;
 }
 

@@ -44,17 +44,20 @@ def draw_discs(spec: HologramSpec) -> np.ndarray:
     return np.ascontiguousarray(np.stack([x, y, d, z], axis=1), dtype=np.float64)
 
 
-def draw_noise(spec: HologramSpec) -> np.ndarray:
-    rng = np.random.Generator(np.random.PCG64(spec.seed + 1))
+def draw_noise(spec: HologramSpec, stream: int = 1) -> np.ndarray:
+    """Sensor noise of the hologram: N(0, sigma^2) from the stream ``seed + stream``."""
+    rng = np.random.Generator(np.random.PCG64(spec.seed + stream))
     return rng.normal(0.0, spec.sigma, (spec.n, spec.n)).astype(np.float32)
 
 
-def synth_hologram(spec: HologramSpec, device: int | None = None, noise: bool = True) -> torch.Tensor:
-    """A Float32 CUDA tensor of shape (n, n): the seeded hologram."""
+def synth_hologram(spec: HologramSpec, device: int | None = None, noise: bool = True,
+                   noise_stream: int = 1) -> torch.Tensor:
+    """A Float32 CUDA tensor of shape (n, n): the seeded hologram (noisy
+    intensities clamped at 0, as a sensor records them)."""
     dev = torch.cuda.current_device() if device is None else device
     out = torch.empty((spec.n, spec.n), dtype=torch.float32, device=f"cuda:{dev}")
     discs = draw_discs(spec)
-    nz = torch.from_numpy(draw_noise(spec)).to(out.device) if noise and spec.sigma > 0 else None
+    nz = torch.from_numpy(draw_noise(spec, noise_stream)).to(out.device) if noise and spec.sigma > 0 else None
     ctx = _lib.default_context(dev)
     ctx.call("ph_synth_hologram", out.data_ptr(), spec.n, spec.n, discs.ctypes.data, int(spec.count),
              float(spec.wavlen), float(spec.dx), float(spec.z_sensor), nz.data_ptr() if nz is not None else None,
@@ -70,10 +73,6 @@ def synth_pair(spec: HologramSpec, separation: float, device: int | None = None)
     ``separation`` further away.  Each gets its own noise."""
     from dataclasses import replace
     h1 = synth_hologram(spec, device)
-    spec2 = replace(spec, z_sensor=spec.z_sensor - separation, seed=spec.seed)
-    # same discs (same seed), independent noise stream
-    out2 = synth_hologram(replace(spec2, sigma=0.0), device, noise=False)
-    if spec.sigma > 0:
-        rng = np.random.Generator(np.random.PCG64(spec.seed + 2))
-        out2 += torch.from_numpy(rng.normal(0.0, spec.sigma, (spec.n, spec.n)).astype(np.float32)).to(out2.device)
-    return h1, out2
+    # same discs (same seed), the second sensor plane, independent noise stream
+    h2 = synth_hologram(replace(spec, z_sensor=spec.z_sensor - separation), device, noise_stream=2)
+    return h1, h2
