@@ -68,6 +68,8 @@ SIGNATURES = {
     "ph_ccl": (_i32, [_vp, _vp, _vp, _i32, _i64, _i64, _vp]),
     "ph_ccl_roots": (_i32, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp, _i64, _vp]),
     "ph_ccl_batch": (_i32, [_vp, _vp, _vp, _i32, _i64, _i64, _i64, _vp]),
+    "ph_ccl_count_noalloc": (_i32, [_vp, _vp, _i64, _vp]),
+    "ph_noalloc_last_error": (ctypes.c_char_p, []),
     "ph_ccl_boxes": (_i32, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp, _i64, _i64, _i64, _vp]),
 }
 

@@ -39,10 +39,12 @@ def test_every_declaration_cites_reference():
     blocks = re.split(r"\n(?=/\*)", text)
     for name in _declared():
         if name in ("ph_create", "ph_destroy", "ph_last_error", "ph_version", "ph_set_option",
-                    "ph_scratch_bytes", "ph_reserve", "ph_kernel_launches", "ph_profile_report"):
+                    "ph_scratch_bytes", "ph_reserve", "ph_kernel_launches", "ph_profile_report",
+                    "ph_noalloc_last_error"):
             continue
         block = next(b for b in blocks if re.search(rf"\b{name}\s*\(", b))
-        assert re.search(r"\.jl:\d+", block) or "No reference counterpart" in block or "no counterpart" in block, name
+        low = block.lower()
+        assert re.search(r"\.jl:\d+", block) or "no reference counterpart" in low or "no counterpart" in low, name
 
 
 def test_null_context_is_rejected(ph):
