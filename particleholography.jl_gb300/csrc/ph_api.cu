@@ -560,22 +560,28 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
         a.ny_out = ny_out;
         a.y0 = y0;
         a.k0 = k0;
+        a.nbatch = nb;
+        a.group = group;
+        a.err = static_cast<int *>(ctx->small);
         PH_TRY(pass(ctx, s, "recon_a",[&] { return launch_recon_a(ny, a, nb, s); }));
         if (kind == RK_PROJ) {
             ReconB<EPI_PROJ> b{};
             b.t = t; b.tw = tw_x; b.proj64 = p64; b.rows = ny_out; b.nx_out = nx_out; b.x0 = 0;
             b.k0 = k0; b.nbatch = nb; b.group = group; b.vol_slice_stride = (long long)nx_out * ny_out;
+            b.err = static_cast<int *>(ctx->small);
             PH_TRY(pass(ctx, s, "recon_b",[&] { return launch_recon_b(nx, b, s); }));
         } else if (kind == RK_CVOL) {
             ReconB<EPI_CVOL> b{};
             b.t = t; b.tw = tw_x; b.vol = vol; b.rows = ny_out; b.nx_out = nx_out; b.x0 = 0;
-            b.k0 = k0; b.nbatch = nb; b.group = 1; b.vol_slice_stride = (long long)nx_out * ny_out;
+            b.k0 = k0; b.nbatch = nb; b.group = group; b.vol_slice_stride = (long long)nx_out * ny_out;
+            b.err = static_cast<int *>(ctx->small);
             PH_TRY(pass(ctx, s, "recon_b",[&] { return launch_recon_b(nx, b, s); }));
         } else {
             ReconB<EPI_VOL> b{};
             b.t = t; b.tw = tw_x; b.vol = vol; b.vol_dtype = vol_dtype; b.proj64 = want_proj ? p64 : nullptr;
             b.rows = ny_out; b.nx_out = nx_out; b.x0 = x0;
             b.k0 = k0; b.nbatch = nb; b.group = group; b.vol_slice_stride = (long long)nx_out * ny_out;
+            b.err = static_cast<int *>(ctx->small);
             PH_TRY(pass(ctx, s, "recon_b",[&] { return launch_recon_b(nx, b, s); }));
         }
     }

@@ -4,7 +4,7 @@
 namespace ph {
 
 cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s) {
-    return launch_len<true>(n, b, b.nx, nbatch, s);
+    return launch_len<true>(n, b, b.nx, (nbatch + b.group - 1) / b.group, s);
 }
 
 }  // namespace ph

@@ -30,7 +30,8 @@ inline int rows_per_cta(int n) {
 template <int N, bool ROW_FAST, class Body>
 cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) {
     auto kern = k_pass<N, ROW_FAST, Body>;
-    constexpr int smem = Shape<N>::template smem_bytes<ROW_FAST>();
+    constexpr size_t smem = Body::template smem<N, ROW_FAST>();
+    static_assert(smem <= kSmemMax, "pass needs more shared memory than a CTA has");
     if constexpr (smem > 48 * 1024) {
         // Per-device opt-in to more than 48 KB of dynamic shared memory.
         static unsigned long long done_mask = 0;

@@ -10,10 +10,16 @@
 //   after a forward row pass  [nx][ny]   (row = kx, along y)
 //   spectrum state            [nx][ny]   float4 (re, im, phase-rate bits, |Hdz|-1)
 //   slice intermediate T      [batch][ny][nx]
+//
+// The reconstruction passes stage their input rows in shared memory with bulk
+// asynchronous copies (TMA, ph_tma.cuh): pass A loads its spectrum-state rows
+// once and transforms several slices from them; pass B double-buffers the rows
+// of the next slice while it transforms the current one.
 #pragma once
 
 #include <cuda_fp16.h>
 #include "ph_fft.cuh"
+#include "ph_tma.cuh"
 
 namespace ph {
 
@@ -29,7 +35,7 @@ struct Shape {
     template <bool ROW_FAST>
     static constexpr int stride() { return SmemRow<N, ROWS, P, ROW_FAST>::STRIDE; }
     template <bool ROW_FAST>
-    static constexpr int smem_bytes() { return ROWS * stride<ROW_FAST>() * 8; }
+    static constexpr size_t smem_bytes() { return (size_t)ROWS * stride<ROW_FAST>() * 8; }
 };
 
 template <int N, bool ROW_FAST>
@@ -38,13 +44,26 @@ struct ThreadMap {
     __device__ __forceinline__ static int j(int t) { return ROW_FAST ? t / Shape<N>::ROWS : t % Shape<N>::P; }
 };
 
+constexpr size_t kSmemMax = 227 * 1024;   // opt-in dynamic shared memory per CTA
+
+// Default shared-memory layout of a pass: one padded exchange row per row.
+struct PassBase {
+    template <int N, bool ROW_FAST>
+    static constexpr size_t smem() { return Shape<N>::template smem_bytes<ROW_FAST>(); }
+};
+
+template <int N, bool ROW_FAST>
+__device__ __forceinline__ float2 *xrow(unsigned char *base, int r) {
+    return reinterpret_cast<float2 *>(base) + (size_t)r * Shape<N>::template stride<ROW_FAST>();
+}
+
 template <int N, bool ROW_FAST, class Body>
 __global__ void __launch_bounds__(Shape<N>::THREADS) k_pass(const Body body) {
-    extern __shared__ float2 ph_smem[];
+    extern __shared__ __align__(128) unsigned char ph_smem[];
     const int t = threadIdx.x;
     const int r = ThreadMap<N, ROW_FAST>::row(t);
     const int j = ThreadMap<N, ROW_FAST>::j(t);
-    body.template run<N>(ph_smem + r * Shape<N>::template stride<ROW_FAST>(), r, j);
+    body.template run<N, ROW_FAST>(ph_smem, r, j);
 }
 
 __device__ __forceinline__ int shift_idx(int i, int n) {   // centred index of natural frequency i
@@ -60,7 +79,7 @@ enum FwdInput { FWD_COMPLEX = 0, FWD_SQRT_REAL = 1, FWD_PADDED = 2 };
 // FWD_PADDED: the input is the virtual 2n x 2n mean-padded array of `src`
 // (n = nx_in) with `src` at rows/cols [pad_off, pad_off + n).
 template <int MODE>
-struct FwdRowsT {
+struct FwdRowsT : PassBase {
     const float2 *src;
     const float *src_real;
     float2 *dst;
@@ -69,14 +88,14 @@ struct FwdRowsT {
     int nrows;                // rows of the (virtual) input = ny
     int nx_in, ny_in, pad_off;
 
-    template <int N>
-    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
         const int y = blockIdx.x * Shape<N>::ROWS + r;
         const bool valid = y < nrows;
         float2 mean = make_float2(0.f, 0.f);
         if (MODE == FWD_PADDED) mean = *pad_mean;
         fft_row<N, Shape<N>::E, false>(
-            srow, j, tw,
+            xrow<N, RF>(smem, r), j, tw,
             [&](int, int x) -> float2 {
                 if (!valid) return make_float2(0.f, 0.f);
                 if constexpr (MODE == FWD_COMPLEX) {
@@ -107,7 +126,7 @@ __device__ __forceinline__ uint32_t phase_turns_u32(float2 h) {
 // Rows kx of the forward-row output, FFT along y, times the front transfer
 // (and 1/(nx ny)), stored with the slice phase rate of the slice transfer:
 // state[kx][ky] = (X0, turns(Hdz), |Hdz| - 1).
-struct SpectrumCols {
+struct SpectrumCols : PassBase {
     const float2 *a1;        // [nx][ny]
     const float2 *hf, *hdz;  // centred [ny][nx]
     float4 *state;           // [nx][ny]
@@ -115,13 +134,13 @@ struct SpectrumCols {
     int nx, ny;
     float scale;
 
-    template <int N>
-    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
         const int kx = blockIdx.x * Shape<N>::ROWS + r;
         const bool valid = kx < nx;
         const int sx = valid ? shift_idx(kx, nx) : 0;
         fft_row<N, Shape<N>::E, false>(
-            srow, j, tw,
+            xrow<N, RF>(smem, r), j, tw,
             [&](int, int y) -> float2 { return valid ? a1[(size_t)kx * N + y] : make_float2(0.f, 0.f); },
             [&](int, int ky, float2 v) {
                 if (!valid) return;
@@ -139,39 +158,90 @@ struct SpectrumCols {
 // Slice k of rows kx: X_k = X0 * Hdz^k evaluated directly from the phase rate
 // (exact integer turn arithmetic) and |Hdz|^k ~ 1 + k (|Hdz| - 1); inverse FFT
 // along ky; transposed store T[b][y - y0][kx] for y in [y0, y0 + ny_out).
+//
+// A CTA loads the spectrum-state rows of its ROWS rows into shared memory once
+// (one bulk copy per row) and transforms `group` consecutive slices from them.
+// The state rows are spaced so that the 16-byte loads of a phase of 8 lanes
+// (ROWS rows x 8/ROWS columns) fall on distinct banks.
 struct ReconA {
     const float4 *state;   // [nx][ny]
     float2 *t;             // [batch][ny_out][nx]
     const float2 *tw;
+    int *err;              // raised if a bulk-copy wait times out
     int nx, ny_out, y0;
     int k0;                // global slice index of batch slot 0
+    int nbatch, group;     // slices in the batch, slices per CTA
 
     template <int N>
-    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
-        const int kx = blockIdx.x * Shape<N>::ROWS + r;
+    static constexpr size_t state_stride() {   // bytes between staged state rows
+        constexpr int R = Shape<N>::ROWS;
+        constexpr size_t dense = (size_t)N * 16;
+        return (dense + 127) / 128 * 128 + (16 * (8 / (R < 8 ? R : 8))) % 128;
+    }
+    // Staged when the state rows and the exchange rows fit the CTA's shared memory.
+    template <int N, bool RF>
+    static constexpr bool staged() {
+        return (size_t)Shape<N>::ROWS * state_stride<N>() + Shape<N>::template smem_bytes<RF>() + 16 <= kSmemMax;
+    }
+    template <int N, bool RF>
+    static constexpr size_t stage_total() { return staged<N, RF>() ? (size_t)Shape<N>::ROWS * state_stride<N>() : 0; }
+    template <int N, bool RF>
+    static constexpr size_t smem() {
+        return stage_total<N, RF>() + Shape<N>::template smem_bytes<RF>() + 16;
+    }
+
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
+        constexpr int ROWS = Shape<N>::ROWS;
+        constexpr size_t SS = state_stride<N>();
+        unsigned char *xbase = smem + stage_total<N, RF>();
+        uint64_t *bar = reinterpret_cast<uint64_t *>(xbase + Shape<N>::template smem_bytes<RF>());
+        const int kx0 = blockIdx.x * ROWS;
+        const int kx = kx0 + r;
         const bool valid = kx < nx;
-        const int b = blockIdx.y;
-        const uint32_t k = (uint32_t)(k0 + b);
-        const float kf = (float)k;
-        float2 *tb = t + (size_t)b * ny_out * nx;
-        fft_row<N, Shape<N>::E, true>(
-            srow, j, tw,
-            [&](int, int ky) -> float2 {
-                if (!valid) return make_float2(0.f, 0.f);
-                const float4 s = state[(size_t)kx * N + ky];
-                const int32_t tt = (int32_t)(k * __float_as_uint(s.z));
-                const float ang = (float)tt * 1.46291807926715968e-9f;   // 2 pi / 2^32
-                float sn, cs;
-                __sincosf(ang, &sn, &cs);
-                const float mag = fmaf(kf, s.w, 1.0f);
-                const float2 g = make_float2(cs * mag, sn * mag);
-                return cmul(make_float2(s.x, s.y), g);
-            },
-            [&](int, int y, float2 v) {
-                const int yo = y - y0;
-                // streaming store: T passes through L2 once; keep the state resident instead
-                if (valid && yo >= 0 && yo < ny_out) __stcs(tb + (size_t)yo * nx + kx, v);
-            });
+        const float4 *srow;
+        if constexpr (staged<N, RF>()) {
+            if (threadIdx.x == 0) {
+                mbar_init(bar, 1);
+                mbar_fence_init();
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const int nvalid = min(ROWS, nx - kx0);
+                mbar_arrive_expect_tx(bar, (uint32_t)(nvalid * N * 16));
+                for (int q = 0; q < nvalid; ++q)
+                    bulk_g2s(smem + (size_t)q * SS, state + (size_t)(kx0 + q) * N, N * 16, bar);
+            }
+            mbar_wait(bar, 0, err);
+            srow = reinterpret_cast<const float4 *>(smem + (size_t)r * SS);
+        } else {
+            srow = state + (size_t)(valid ? kx : 0) * N;
+        }
+        float2 *xr = xrow<N, RF>(xbase, r);
+        const int b0 = blockIdx.y * group;
+        const int b1 = min(b0 + group, nbatch);
+        for (int b = b0; b < b1; ++b) {
+            const uint32_t k = (uint32_t)(k0 + b);
+            const float kf = (float)k;
+            float2 *tb = t + (size_t)b * ny_out * nx;
+            fft_row<N, Shape<N>::E, true>(
+                xr, j, tw,
+                [&](int, int ky) -> float2 {
+                    const float4 s = srow[ky];
+                    const int32_t tt = (int32_t)(k * __float_as_uint(s.z));
+                    const float ang = (float)tt * 1.46291807926715968e-9f;   // 2 pi / 2^32
+                    float sn, cs;
+                    __sincosf(ang, &sn, &cs);
+                    const float mag = fmaf(kf, s.w, 1.0f);
+                    const float2 g = make_float2(cs * mag, sn * mag);
+                    return cmul(make_float2(s.x, s.y), g);
+                },
+                [&](int, int y, float2 v) {
+                    const int yo = y - y0;
+                    // streaming store: T passes through L2 once
+                    if (valid && yo >= 0 && yo < ny_out) __stcs(tb + (size_t)yo * nx + kx, v);
+                });
+        }
     }
 };
 
@@ -188,26 +258,66 @@ __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f),
 // Rows y of T, inverse FFT along kx, |u|^2 and the epilogue.  A CTA handles
 // ROWS rows for `group` consecutive batch slots; with EPI_PROJ the running
 // minimum stays in registers across them and is merged with one atomicMin of
-// (float bits << 32 | slice) per pixel.
+// (float bits << 32 | slice) per pixel.  The rows of slice b+1 arrive in
+// shared memory by bulk copy while slice b is transformed (two buffers).
 template <int EPI>
 struct ReconB {
     const float2 *t;                 // [batch][rows][nx]
     const float2 *tw;
     unsigned long long *proj64;      // [rows_out][nx_out] or null
     void *vol;                       // [S][rows_out][nx_out] or null
+    int *err;                        // raised if a bulk-copy wait times out
     int vol_dtype;
     int rows;                        // rows of T per slice
     int nx_out, x0;                  // stored columns [x0, x0 + nx_out)
     int k0, nbatch, group;
     long long vol_slice_stride;      // elements per stored slice
 
-    template <int N>
-    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+    // Staged when a row is a multiple of 16 bytes (bulk-copy granularity) and two
+    // stage buffers plus the exchange rows fit the CTA's shared memory.
+    template <int N, bool RF>
+    static constexpr bool staged() {
+        return N % 2 == 0 &&
+               2 * (size_t)Shape<N>::ROWS * N * 8 + Shape<N>::template smem_bytes<RF>() + 16 <= kSmemMax;
+    }
+    template <int N, bool RF>
+    static constexpr size_t stage_bytes() { return staged<N, RF>() ? (size_t)Shape<N>::ROWS * N * 8 : 0; }
+    template <int N, bool RF>
+    static constexpr size_t smem() {
+        return 2 * stage_bytes<N, RF>() + Shape<N>::template smem_bytes<RF>() + 16;
+    }
+
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
         constexpr int E = Shape<N>::E;
-        const int y = blockIdx.x * Shape<N>::ROWS + r;
+        constexpr int ROWS = Shape<N>::ROWS;
+        constexpr size_t SB = stage_bytes<N, RF>();
+        unsigned char *xbase = smem + 2 * SB;
+        uint64_t *bars = reinterpret_cast<uint64_t *>(xbase + Shape<N>::template smem_bytes<RF>());
+        float2 *xr = xrow<N, RF>(xbase, r);
+        const int yb = blockIdx.x * ROWS;
+        const int y = yb + r;
         const bool valid = y < rows;
         const int b0 = blockIdx.y * group;
         const int b1 = min(b0 + group, nbatch);
+        const int nvalid = min(ROWS, rows - yb);
+        auto issue = [&](int b, int buf) {   // one thread: the rows of slice b into buffer buf
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(bars + buf, (uint32_t)(nvalid * N * 8));
+            for (int q = 0; q < nvalid; ++q)
+                bulk_g2s(smem + buf * SB + (size_t)q * N * 8, t + ((size_t)b * rows + yb + q) * N, N * 8, bars + buf);
+        };
+        if constexpr (staged<N, RF>()) {
+            if (threadIdx.x == 0) {
+                mbar_init(bars, 1);
+                mbar_init(bars + 1, 1);
+                mbar_fence_init();
+            }
+            __syncthreads();
+            if (threadIdx.x == 0 && b0 < b1) issue(b0, 0);
+        }
+        uint32_t parity = 0;   // bit q: parity of the next completion of buffer q
+
         float minv[E];
         int mink[E];
 #pragma unroll
@@ -216,14 +326,23 @@ struct ReconB {
 
         for (int b = b0; b < b1; ++b) {
             const int k = k0 + b;
-            const float2 *tb = t + ((size_t)b * rows + (valid ? y : 0)) * N;
+            const int buf = (b - b0) & 1;
+            const float2 *in;
+            if constexpr (staged<N, RF>()) {
+                // the other buffer was last read before this iteration's barriers: refill it
+                if (threadIdx.x == 0 && b + 1 < b1) issue(b + 1, buf ^ 1);
+                mbar_wait(bars + buf, (parity >> buf) & 1u, err);
+                parity ^= 1u << buf;
+                in = reinterpret_cast<const float2 *>(smem + buf * SB) + (size_t)r * N;
+            } else {
+                in = t + ((size_t)b * rows + (valid ? y : 0)) * N;
+            }
             fft_row<N, E, true>(
-                srow, j, tw,
-                [&](int, int kx) -> float2 { return valid ? __ldcs(tb + kx) : make_float2(0.f, 0.f); },
+                xr, j, tw, [&](int, int kx) -> float2 { return in[kx]; },
                 [&](int slot, int x, float2 v) {
                     if constexpr (EPI == EPI_PROJ) {
-                        const float in = fmaf(v.x, v.x, v.y * v.y);
-                        if (in < minv[slot]) { minv[slot] = in; mink[slot] = k; }
+                        const float i2 = fmaf(v.x, v.x, v.y * v.y);
+                        if (i2 < minv[slot]) { minv[slot] = i2; mink[slot] = k; }
                     } else {
                         const int xo = x - x0;
                         if (!valid || xo < 0 || xo >= nx_out) return;
@@ -231,28 +350,28 @@ struct ReconB {
                         if constexpr (EPI == EPI_CVOL) {
                             reinterpret_cast<float2 *>(vol)[o] = v;
                         } else {
-                            const float in = clamp01(fmaf(v.x, v.x, v.y * v.y));
+                            const float i2 = clamp01(fmaf(v.x, v.x, v.y * v.y));
                             float stored;
                             switch (vol_dtype) {
                                 case 0: {   // N0f8
-                                    const unsigned q = __float2uint_rn(in * 255.0f);
+                                    const unsigned q = __float2uint_rn(i2 * 255.0f);
                                     reinterpret_cast<uint8_t *>(vol)[o] = (uint8_t)q;
                                     stored = __fdiv_rn((float)q, 255.0f);
                                     break;
                                 }
                                 case 1: {
-                                    const __half h = __float2half_rn(in);
+                                    const __half h = __float2half_rn(i2);
                                     reinterpret_cast<__half *>(vol)[o] = h;
                                     stored = __half2float(h);
                                     break;
                                 }
                                 case 3:
-                                    reinterpret_cast<double *>(vol)[o] = (double)in;
-                                    stored = in;
+                                    reinterpret_cast<double *>(vol)[o] = (double)i2;
+                                    stored = i2;
                                     break;
                                 default:
-                                    reinterpret_cast<float *>(vol)[o] = in;
-                                    stored = in;
+                                    reinterpret_cast<float *>(vol)[o] = i2;
+                                    stored = i2;
                                     break;
                             }
                             if (track_min && stored < minv[slot]) { minv[slot] = stored; mink[slot] = k; }
@@ -288,7 +407,7 @@ __device__ __forceinline__ float2 amplitude_replace(float2 u, float s) {
 
 // Rows y of [y][kx] data (row length nx).
 template <int MODE>
-struct GsRow {
+struct GsRow : PassBase {
     const float2 *src;       // [ny][nx]
     const float *holo;       // [ny][nx] intensity whose sqrt replaces the amplitude
     float2 *dst;             // MID: [nx][ny]; FINAL / INV: [ny][nx]
@@ -296,9 +415,10 @@ struct GsRow {
     double *resid;           // nullable: [0] += (|u| - s)^2, [1] += s^2
     int nrows;
 
-    template <int N>
-    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
         constexpr int E = Shape<N>::E;
+        float2 *srow = xrow<N, RF>(smem, r);
         const int y = blockIdx.x * Shape<N>::ROWS + r;
         const bool valid = y < nrows;
         const float2 *in = src + (size_t)(valid ? y : 0) * N;
@@ -346,7 +466,7 @@ struct GsRow {
 // Rows kx of [kx][y] data (row length ny): forward FFT along y, times the
 // centred transfer (and `scale`), inverse FFT along y, transposed store [y][kx].
 // With `mask` (real, centred) instead of `h`, the multiplier is the mask.
-struct GsCol {
+struct GsCol : PassBase {
     const float2 *src;       // [nx][ny]
     const float2 *h;         // centred [ny][nx] (or null)
     const float *mask;       // centred [ny][nx] (or null)
@@ -355,9 +475,10 @@ struct GsCol {
     int nx;
     float scale;
 
-    template <int N>
-    __device__ __forceinline__ void run(float2 *srow, int r, int j) const {
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
         constexpr int E = Shape<N>::E;
+        float2 *srow = xrow<N, RF>(smem, r);
         const int kx = blockIdx.x * Shape<N>::ROWS + r;
         const bool valid = kx < nx;
         const int sx = valid ? shift_idx(kx, nx) : 0;
