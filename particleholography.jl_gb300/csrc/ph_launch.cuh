@@ -44,8 +44,9 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) 
             __atomic_fetch_or(&done_mask, bit, __ATOMIC_ACQ_REL);
         }
     }
-    dim3 grid((nrows + Shape<N>::ROWS - 1) / Shape<N>::ROWS, grid_y);
-    kern<<<grid, Shape<N>::THREADS, smem, s>>>(body);
+    using S = Shape<N, Body::EPT>;
+    dim3 grid((nrows + S::ROWS - 1) / S::ROWS, grid_y);
+    kern<<<grid, S::THREADS, smem, s>>>(body);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,10 @@
 // asynchronous copies (TMA, ph_tma.cuh): pass A loads its spectrum-state rows
 // once and transforms several slices from them; pass B double-buffers the rows
 // of the next slice while it transforms the current one.
+//
+// Each pass chooses its elements per thread (EPT, the main radix) and the CTAs
+// per SM it asks the register allocator for (MINB): fewer values per thread
+// buy more resident warps where the pass is latency-bound.
 #pragma once
 
 #include <cuda_fp16.h>
@@ -25,10 +29,14 @@ namespace ph {
 
 // ---------------------------------------------------------------- launch shape
 
-template <int N>
+// Shape of a pass over rows of length N with (up to) EPT values per thread:
+// E values per thread (3 * EPT/2 for N = 3 * 2^a), P threads per row, ROWS rows
+// and THREADS = ROWS * P threads (512 for every large N) per CTA.
+template <int N, int EPT = 16>
 struct Shape {
     static constexpr bool POW2 = (N & (N - 1)) == 0;
-    static constexpr int E = POW2 ? (N < 16 ? N : 16) : (N < 24 ? N : 24);
+    static constexpr int EREQ = POW2 ? EPT : 3 * (EPT / 2);
+    static constexpr int E = N < EREQ ? N : EREQ;
     static constexpr int P = N / E;
     static constexpr int ROWS = cmax(1, cmin(64, 512 / P));
     static constexpr int THREADS = ROWS * P;
@@ -38,31 +46,35 @@ struct Shape {
     static constexpr size_t smem_bytes() { return (size_t)ROWS * stride<ROW_FAST>() * 8; }
 };
 
-template <int N, bool ROW_FAST>
+template <int N, int EPT, bool ROW_FAST>
 struct ThreadMap {
-    __device__ __forceinline__ static int row(int t) { return ROW_FAST ? t % Shape<N>::ROWS : t / Shape<N>::P; }
-    __device__ __forceinline__ static int j(int t) { return ROW_FAST ? t / Shape<N>::ROWS : t % Shape<N>::P; }
+    using S = Shape<N, EPT>;
+    __device__ __forceinline__ static int row(int t) { return ROW_FAST ? t % S::ROWS : t / S::P; }
+    __device__ __forceinline__ static int j(int t) { return ROW_FAST ? t / S::ROWS : t % S::P; }
 };
 
 constexpr size_t kSmemMax = 227 * 1024;   // opt-in dynamic shared memory per CTA
 
-// Default shared-memory layout of a pass: one padded exchange row per row.
+// Defaults of a pass: radix-16 engine, one CTA per SM of register budget, one
+// padded exchange row per transformed row of shared memory.
 struct PassBase {
+    static constexpr int EPT = 16;
+    static constexpr int MINB = 1;
     template <int N, bool ROW_FAST>
-    static constexpr size_t smem() { return Shape<N>::template smem_bytes<ROW_FAST>(); }
+    static constexpr size_t smem() { return Shape<N, EPT>::template smem_bytes<ROW_FAST>(); }
 };
 
-template <int N, bool ROW_FAST>
+template <int N, int EPT, bool ROW_FAST>
 __device__ __forceinline__ float2 *xrow(unsigned char *base, int r) {
-    return reinterpret_cast<float2 *>(base) + (size_t)r * Shape<N>::template stride<ROW_FAST>();
+    return reinterpret_cast<float2 *>(base) + (size_t)r * Shape<N, EPT>::template stride<ROW_FAST>();
 }
 
 template <int N, bool ROW_FAST, class Body>
-__global__ void __launch_bounds__(Shape<N>::THREADS) k_pass(const Body body) {
+__global__ void __launch_bounds__(Shape<N, Body::EPT>::THREADS, Body::MINB) k_pass(const Body body) {
     extern __shared__ __align__(128) unsigned char ph_smem[];
     const int t = threadIdx.x;
-    const int r = ThreadMap<N, ROW_FAST>::row(t);
-    const int j = ThreadMap<N, ROW_FAST>::j(t);
+    const int r = ThreadMap<N, Body::EPT, ROW_FAST>::row(t);
+    const int j = ThreadMap<N, Body::EPT, ROW_FAST>::j(t);
     body.template run<N, ROW_FAST>(ph_smem, r, j);
 }
 
@@ -90,12 +102,13 @@ struct FwdRowsT : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        const int y = blockIdx.x * Shape<N>::ROWS + r;
+        using S = Shape<N, EPT>;
+        const int y = blockIdx.x * S::ROWS + r;
         const bool valid = y < nrows;
         float2 mean = make_float2(0.f, 0.f);
         if (MODE == FWD_PADDED) mean = *pad_mean;
-        fft_row<N, Shape<N>::E, false>(
-            xrow<N, RF>(smem, r), j, tw,
+        fft_row<N, S::E, false>(
+            xrow<N, EPT, RF>(smem, r), j, tw,
             [&](int, int x) -> float2 {
                 if (!valid) return make_float2(0.f, 0.f);
                 if constexpr (MODE == FWD_COMPLEX) {
@@ -136,11 +149,12 @@ struct SpectrumCols : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        const int kx = blockIdx.x * Shape<N>::ROWS + r;
+        using S = Shape<N, EPT>;
+        const int kx = blockIdx.x * S::ROWS + r;
         const bool valid = kx < nx;
         const int sx = valid ? shift_idx(kx, nx) : 0;
-        fft_row<N, Shape<N>::E, false>(
-            xrow<N, RF>(smem, r), j, tw,
+        fft_row<N, S::E, false>(
+            xrow<N, EPT, RF>(smem, r), j, tw,
             [&](int, int y) -> float2 { return valid ? a1[(size_t)kx * N + y] : make_float2(0.f, 0.f); },
             [&](int, int ky, float2 v) {
                 if (!valid) return;
@@ -163,7 +177,7 @@ struct SpectrumCols : PassBase {
 // (one bulk copy per row) and transforms `group` consecutive slices from them.
 // The state rows are spaced so that the 16-byte loads of a phase of 8 lanes
 // (ROWS rows x 8/ROWS columns) fall on distinct banks.
-struct ReconA {
+struct ReconA : PassBase {
     const float4 *state;   // [nx][ny]
     float2 *t;             // [batch][ny_out][nx]
     const float2 *tw;
@@ -174,28 +188,32 @@ struct ReconA {
 
     template <int N>
     static constexpr size_t state_stride() {   // bytes between staged state rows
-        constexpr int R = Shape<N>::ROWS;
+        constexpr int R = Shape<N, EPT>::ROWS;
         constexpr size_t dense = (size_t)N * 16;
         return (dense + 127) / 128 * 128 + (16 * (8 / (R < 8 ? R : 8))) % 128;
     }
-    // Staged when the state rows and the exchange rows fit the CTA's shared memory.
+    // Staged when MINB CTAs with their state rows and exchange rows fit an SM.
     template <int N, bool RF>
     static constexpr bool staged() {
-        return (size_t)Shape<N>::ROWS * state_stride<N>() + Shape<N>::template smem_bytes<RF>() + 16 <= kSmemMax;
+        return MINB * ((size_t)Shape<N, EPT>::ROWS * state_stride<N>() + Shape<N, EPT>::template smem_bytes<RF>() +
+                       16) <= kSmemMax;
     }
     template <int N, bool RF>
-    static constexpr size_t stage_total() { return staged<N, RF>() ? (size_t)Shape<N>::ROWS * state_stride<N>() : 0; }
+    static constexpr size_t stage_total() {
+        return staged<N, RF>() ? (size_t)Shape<N, EPT>::ROWS * state_stride<N>() : 0;
+    }
     template <int N, bool RF>
     static constexpr size_t smem() {
-        return stage_total<N, RF>() + Shape<N>::template smem_bytes<RF>() + 16;
+        return stage_total<N, RF>() + Shape<N, EPT>::template smem_bytes<RF>() + 16;
     }
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        constexpr int ROWS = Shape<N>::ROWS;
+        using S = Shape<N, EPT>;
+        constexpr int ROWS = S::ROWS;
         constexpr size_t SS = state_stride<N>();
         unsigned char *xbase = smem + stage_total<N, RF>();
-        uint64_t *bar = reinterpret_cast<uint64_t *>(xbase + Shape<N>::template smem_bytes<RF>());
+        uint64_t *bar = reinterpret_cast<uint64_t *>(xbase + S::template smem_bytes<RF>());
         const int kx0 = blockIdx.x * ROWS;
         const int kx = kx0 + r;
         const bool valid = kx < nx;
@@ -217,14 +235,14 @@ struct ReconA {
         } else {
             srow = state + (size_t)(valid ? kx : 0) * N;
         }
-        float2 *xr = xrow<N, RF>(xbase, r);
+        float2 *xr = xrow<N, EPT, RF>(xbase, r);
         const int b0 = blockIdx.y * group;
         const int b1 = min(b0 + group, nbatch);
         for (int b = b0; b < b1; ++b) {
             const uint32_t k = (uint32_t)(k0 + b);
             const float kf = (float)k;
             float2 *tb = t + (size_t)b * ny_out * nx;
-            fft_row<N, Shape<N>::E, true>(
+            fft_row<N, S::E, true>(
                 xr, j, tw,
                 [&](int, int ky) -> float2 {
                     const float4 s = srow[ky];
@@ -260,8 +278,12 @@ __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f),
 // minimum stays in registers across them and is merged with one atomicMin of
 // (float bits << 32 | slice) per pixel.  The rows of slice b+1 arrive in
 // shared memory by bulk copy while slice b is transformed (two buffers).
+// Radix-8 stages (8 values per thread) keep the registers at 64 so that two
+// CTAs (32 warps) share an SM: the pass is latency-bound, not issue-bound.
 template <int EPI>
-struct ReconB {
+struct ReconB : PassBase {
+    static constexpr int EPT = 8;
+    static constexpr int MINB = 2;
     const float2 *t;                 // [batch][rows][nx]
     const float2 *tw;
     unsigned long long *proj64;      // [rows_out][nx_out] or null
@@ -273,28 +295,29 @@ struct ReconB {
     int k0, nbatch, group;
     long long vol_slice_stride;      // elements per stored slice
 
-    // Staged when a row is a multiple of 16 bytes (bulk-copy granularity) and two
-    // stage buffers plus the exchange rows fit the CTA's shared memory.
+    // Staged when a row is a multiple of 16 bytes (bulk-copy granularity) and
+    // MINB CTAs with two stage buffers plus the exchange rows fit an SM.
     template <int N, bool RF>
     static constexpr bool staged() {
-        return N % 2 == 0 &&
-               2 * (size_t)Shape<N>::ROWS * N * 8 + Shape<N>::template smem_bytes<RF>() + 16 <= kSmemMax;
+        return N % 2 == 0 && MINB * (2 * (size_t)Shape<N, EPT>::ROWS * N * 8 +
+                                     Shape<N, EPT>::template smem_bytes<RF>() + 16) <= kSmemMax;
     }
     template <int N, bool RF>
-    static constexpr size_t stage_bytes() { return staged<N, RF>() ? (size_t)Shape<N>::ROWS * N * 8 : 0; }
+    static constexpr size_t stage_bytes() { return staged<N, RF>() ? (size_t)Shape<N, EPT>::ROWS * N * 8 : 0; }
     template <int N, bool RF>
     static constexpr size_t smem() {
-        return 2 * stage_bytes<N, RF>() + Shape<N>::template smem_bytes<RF>() + 16;
+        return 2 * stage_bytes<N, RF>() + Shape<N, EPT>::template smem_bytes<RF>() + 16;
     }
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        constexpr int E = Shape<N>::E;
-        constexpr int ROWS = Shape<N>::ROWS;
+        using S = Shape<N, EPT>;
+        constexpr int E = S::E;
+        constexpr int ROWS = S::ROWS;
         constexpr size_t SB = stage_bytes<N, RF>();
         unsigned char *xbase = smem + 2 * SB;
-        uint64_t *bars = reinterpret_cast<uint64_t *>(xbase + Shape<N>::template smem_bytes<RF>());
-        float2 *xr = xrow<N, RF>(xbase, r);
+        uint64_t *bars = reinterpret_cast<uint64_t *>(xbase + S::template smem_bytes<RF>());
+        float2 *xr = xrow<N, EPT, RF>(xbase, r);
         const int yb = blockIdx.x * ROWS;
         const int y = yb + r;
         const bool valid = y < rows;
@@ -417,9 +440,10 @@ struct GsRow : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        constexpr int E = Shape<N>::E;
-        float2 *srow = xrow<N, RF>(smem, r);
-        const int y = blockIdx.x * Shape<N>::ROWS + r;
+        using S = Shape<N, EPT>;
+        constexpr int E = S::E;
+        float2 *srow = xrow<N, EPT, RF>(smem, r);
+        const int y = blockIdx.x * S::ROWS + r;
         const bool valid = y < nrows;
         const float2 *in = src + (size_t)(valid ? y : 0) * N;
         auto ld = [&](int, int x) -> float2 { return valid ? in[x] : make_float2(0.f, 0.f); };
@@ -477,9 +501,10 @@ struct GsCol : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        constexpr int E = Shape<N>::E;
-        float2 *srow = xrow<N, RF>(smem, r);
-        const int kx = blockIdx.x * Shape<N>::ROWS + r;
+        using S = Shape<N, EPT>;
+        constexpr int E = S::E;
+        float2 *srow = xrow<N, EPT, RF>(smem, r);
+        const int kx = blockIdx.x * S::ROWS + r;
         const bool valid = kx < nx;
         const int sx = valid ? shift_idx(kx, nx) : 0;
         const float2 *in = src + (size_t)(valid ? kx : 0) * N;
