@@ -44,7 +44,7 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) 
             __atomic_fetch_or(&done_mask, bit, __ATOMIC_ACQ_REL);
         }
     }
-    using S = Shape<N, Body::EPT>;
+    using S = Shape<N, Body::EPT, Body::TT>;
     dim3 grid((nrows + S::ROWS - 1) / S::ROWS, grid_y);
     kern<<<grid, S::THREADS, smem, s>>>(body);
     return cudaGetLastError();

@@ -32,13 +32,13 @@ namespace ph {
 // Shape of a pass over rows of length N with (up to) EPT values per thread:
 // E values per thread (3 * EPT/2 for N = 3 * 2^a), P threads per row, ROWS rows
 // and THREADS = ROWS * P threads (512 for every large N) per CTA.
-template <int N, int EPT = 16>
+template <int N, int EPT = 16, int TT = 512>
 struct Shape {
     static constexpr bool POW2 = (N & (N - 1)) == 0;
     static constexpr int EREQ = POW2 ? EPT : 3 * (EPT / 2);
     static constexpr int E = N < EREQ ? N : EREQ;
     static constexpr int P = N / E;
-    static constexpr int ROWS = cmax(1, cmin(64, 512 / P));
+    static constexpr int ROWS = cmax(1, cmin(64, TT / P));
     static constexpr int THREADS = ROWS * P;
     template <bool ROW_FAST>
     static constexpr int stride() { return SmemRow<N, ROWS, P, ROW_FAST>::STRIDE; }
@@ -46,9 +46,9 @@ struct Shape {
     static constexpr size_t smem_bytes() { return (size_t)ROWS * stride<ROW_FAST>() * 8; }
 };
 
-template <int N, int EPT, bool ROW_FAST>
+template <int N, int EPT, int TT, bool ROW_FAST>
 struct ThreadMap {
-    using S = Shape<N, EPT>;
+    using S = Shape<N, EPT, TT>;
     __device__ __forceinline__ static int row(int t) { return ROW_FAST ? t % S::ROWS : t / S::P; }
     __device__ __forceinline__ static int j(int t) { return ROW_FAST ? t / S::ROWS : t % S::P; }
 };
@@ -59,22 +59,30 @@ constexpr size_t kSmemMax = 227 * 1024;   // opt-in dynamic shared memory per CT
 // padded exchange row per transformed row of shared memory.
 struct PassBase {
     static constexpr int EPT = 16;
+    static constexpr int TT = 512;    // target threads per CTA
     static constexpr int MINB = 1;
     template <int N, bool ROW_FAST>
-    static constexpr size_t smem() { return Shape<N, EPT>::template smem_bytes<ROW_FAST>(); }
+    static constexpr size_t smem() { return Shape<N, EPT, TT>::template smem_bytes<ROW_FAST>(); }
 };
 
-template <int N, int EPT, bool ROW_FAST>
+template <int N, int EPT, int TT, bool ROW_FAST>
 __device__ __forceinline__ float2 *xrow(unsigned char *base, int r) {
-    return reinterpret_cast<float2 *>(base) + (size_t)r * Shape<N, EPT>::template stride<ROW_FAST>();
+    return reinterpret_cast<float2 *>(base) + (size_t)r * Shape<N, EPT, TT>::template stride<ROW_FAST>();
+}
+
+// Register budget: MINB x 512 resident threads per SM.
+template <int N, class Body>
+constexpr int min_blocks() {
+    return cmax(1, Body::MINB * 512 / Shape<N, Body::EPT, Body::TT>::THREADS);
 }
 
 template <int N, bool ROW_FAST, class Body>
-__global__ void __launch_bounds__(Shape<N, Body::EPT>::THREADS, Body::MINB) k_pass(const Body body) {
+__global__ void __launch_bounds__(Shape<N, Body::EPT, Body::TT>::THREADS, min_blocks<N, Body>())
+    k_pass(const Body body) {
     extern __shared__ __align__(128) unsigned char ph_smem[];
     const int t = threadIdx.x;
-    const int r = ThreadMap<N, Body::EPT, ROW_FAST>::row(t);
-    const int j = ThreadMap<N, Body::EPT, ROW_FAST>::j(t);
+    const int r = ThreadMap<N, Body::EPT, Body::TT, ROW_FAST>::row(t);
+    const int j = ThreadMap<N, Body::EPT, Body::TT, ROW_FAST>::j(t);
     body.template run<N, ROW_FAST>(ph_smem, r, j);
 }
 
@@ -102,13 +110,13 @@ struct FwdRowsT : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        using S = Shape<N, EPT>;
+        using S = Shape<N, EPT, TT>;
         const int y = blockIdx.x * S::ROWS + r;
         const bool valid = y < nrows;
         float2 mean = make_float2(0.f, 0.f);
         if (MODE == FWD_PADDED) mean = *pad_mean;
         fft_row<N, S::E, false>(
-            xrow<N, EPT, RF>(smem, r), j, tw,
+            xrow<N, EPT, TT, RF>(smem, r), j, tw,
             [&](int, int x) -> float2 {
                 if (!valid) return make_float2(0.f, 0.f);
                 if constexpr (MODE == FWD_COMPLEX) {
@@ -149,12 +157,12 @@ struct SpectrumCols : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        using S = Shape<N, EPT>;
+        using S = Shape<N, EPT, TT>;
         const int kx = blockIdx.x * S::ROWS + r;
         const bool valid = kx < nx;
         const int sx = valid ? shift_idx(kx, nx) : 0;
         fft_row<N, S::E, false>(
-            xrow<N, EPT, RF>(smem, r), j, tw,
+            xrow<N, EPT, TT, RF>(smem, r), j, tw,
             [&](int, int y) -> float2 { return valid ? a1[(size_t)kx * N + y] : make_float2(0.f, 0.f); },
             [&](int, int ky, float2 v) {
                 if (!valid) return;
@@ -188,28 +196,28 @@ struct ReconA : PassBase {
 
     template <int N>
     static constexpr size_t state_stride() {   // bytes between staged state rows
-        constexpr int R = Shape<N, EPT>::ROWS;
+        constexpr int R = Shape<N, EPT, TT>::ROWS;
         constexpr size_t dense = (size_t)N * 16;
         return (dense + 127) / 128 * 128 + (16 * (8 / (R < 8 ? R : 8))) % 128;
     }
     // Staged when MINB CTAs with their state rows and exchange rows fit an SM.
     template <int N, bool RF>
     static constexpr bool staged() {
-        return MINB * ((size_t)Shape<N, EPT>::ROWS * state_stride<N>() + Shape<N, EPT>::template smem_bytes<RF>() +
+        return MINB * ((size_t)Shape<N, EPT, TT>::ROWS * state_stride<N>() + Shape<N, EPT, TT>::template smem_bytes<RF>() +
                        16) <= kSmemMax;
     }
     template <int N, bool RF>
     static constexpr size_t stage_total() {
-        return staged<N, RF>() ? (size_t)Shape<N, EPT>::ROWS * state_stride<N>() : 0;
+        return staged<N, RF>() ? (size_t)Shape<N, EPT, TT>::ROWS * state_stride<N>() : 0;
     }
     template <int N, bool RF>
     static constexpr size_t smem() {
-        return stage_total<N, RF>() + Shape<N, EPT>::template smem_bytes<RF>() + 16;
+        return stage_total<N, RF>() + Shape<N, EPT, TT>::template smem_bytes<RF>() + 16;
     }
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        using S = Shape<N, EPT>;
+        using S = Shape<N, EPT, TT>;
         constexpr int ROWS = S::ROWS;
         constexpr size_t SS = state_stride<N>();
         unsigned char *xbase = smem + stage_total<N, RF>();
@@ -235,7 +243,7 @@ struct ReconA : PassBase {
         } else {
             srow = state + (size_t)(valid ? kx : 0) * N;
         }
-        float2 *xr = xrow<N, EPT, RF>(xbase, r);
+        float2 *xr = xrow<N, EPT, TT, RF>(xbase, r);
         const int b0 = blockIdx.y * group;
         const int b1 = min(b0 + group, nbatch);
         for (int b = b0; b < b1; ++b) {
@@ -278,12 +286,12 @@ __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f),
 // minimum stays in registers across them and is merged with one atomicMin of
 // (float bits << 32 | slice) per pixel.  The rows of slice b+1 arrive in
 // shared memory by bulk copy while slice b is transformed (two buffers).
-// Radix-8 stages (8 values per thread) keep the registers at 64 so that two
-// CTAs (32 warps) share an SM: the pass is latency-bound, not issue-bound.
+// CTAs are small (128 threads: one row at N >= 2048) so that the barriers of
+// the FFT stages span only the warps that exchange data, and four CTAs share
+// an SM.
 template <int EPI>
 struct ReconB : PassBase {
-    static constexpr int EPT = 8;
-    static constexpr int MINB = 2;
+    static constexpr int TT = 128;   // one row per CTA at N >= 2048: barriers span one row's warps
     const float2 *t;                 // [batch][rows][nx]
     const float2 *tw;
     unsigned long long *proj64;      // [rows_out][nx_out] or null
@@ -299,25 +307,25 @@ struct ReconB : PassBase {
     // MINB CTAs with two stage buffers plus the exchange rows fit an SM.
     template <int N, bool RF>
     static constexpr bool staged() {
-        return N % 2 == 0 && MINB * (2 * (size_t)Shape<N, EPT>::ROWS * N * 8 +
-                                     Shape<N, EPT>::template smem_bytes<RF>() + 16) <= kSmemMax;
+        return N % 2 == 0 && MINB * (2 * (size_t)Shape<N, EPT, TT>::ROWS * N * 8 +
+                                     Shape<N, EPT, TT>::template smem_bytes<RF>() + 16) <= kSmemMax;
     }
     template <int N, bool RF>
-    static constexpr size_t stage_bytes() { return staged<N, RF>() ? (size_t)Shape<N, EPT>::ROWS * N * 8 : 0; }
+    static constexpr size_t stage_bytes() { return staged<N, RF>() ? (size_t)Shape<N, EPT, TT>::ROWS * N * 8 : 0; }
     template <int N, bool RF>
     static constexpr size_t smem() {
-        return 2 * stage_bytes<N, RF>() + Shape<N, EPT>::template smem_bytes<RF>() + 16;
+        return 2 * stage_bytes<N, RF>() + Shape<N, EPT, TT>::template smem_bytes<RF>() + 16;
     }
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        using S = Shape<N, EPT>;
+        using S = Shape<N, EPT, TT>;
         constexpr int E = S::E;
         constexpr int ROWS = S::ROWS;
         constexpr size_t SB = stage_bytes<N, RF>();
         unsigned char *xbase = smem + 2 * SB;
         uint64_t *bars = reinterpret_cast<uint64_t *>(xbase + S::template smem_bytes<RF>());
-        float2 *xr = xrow<N, EPT, RF>(xbase, r);
+        float2 *xr = xrow<N, EPT, TT, RF>(xbase, r);
         const int yb = blockIdx.x * ROWS;
         const int y = yb + r;
         const bool valid = y < rows;
@@ -440,9 +448,9 @@ struct GsRow : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        using S = Shape<N, EPT>;
+        using S = Shape<N, EPT, TT>;
         constexpr int E = S::E;
-        float2 *srow = xrow<N, EPT, RF>(smem, r);
+        float2 *srow = xrow<N, EPT, TT, RF>(smem, r);
         const int y = blockIdx.x * S::ROWS + r;
         const bool valid = y < nrows;
         const float2 *in = src + (size_t)(valid ? y : 0) * N;
@@ -501,9 +509,9 @@ struct GsCol : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        using S = Shape<N, EPT>;
+        using S = Shape<N, EPT, TT>;
         constexpr int E = S::E;
-        float2 *srow = xrow<N, EPT, RF>(smem, r);
+        float2 *srow = xrow<N, EPT, TT, RF>(smem, r);
         const int kx = blockIdx.x * S::ROWS + r;
         const bool valid = kx < nx;
         const int sx = valid ? shift_idx(kx, nx) : 0;
