@@ -49,6 +49,11 @@ CONFIGS = {
     "c3": dict(n=4096, slices=1024, dz=(200000.0 - 5000.0) / 1024, z0=5000.0, discs=3000, dmin=10.0, dmax=60.0,
                zmin=5000.0, zmax=200000.0, gs_iters=0, gs_sep=0.0, threshold=0.1, seed=3,
                workload="gabor4096_recon1024_ccl"),
+    # the 2048^2 frame cut to one reconstruction batch (64 slices) and 2 GS iterations: every
+    # kernel launch has the size of its launches in c2; sized for ncu captures (~3 GB on the device)
+    "p2": dict(n=2048, slices=64, dz=200.0, z0=5000.0, discs=800, dmin=10.0, dmax=60.0, zmin=5000.0,
+               zmax=100000.0, gs_iters=2, gs_sep=5000.0, threshold=0.1, seed=2,
+               workload="gs2048_pr2_recon64_profile"),
 }
 L2_FLUSH_BYTES = 512 << 20
 

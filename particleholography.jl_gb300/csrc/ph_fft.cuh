@@ -87,17 +87,30 @@ __device__ __forceinline__ float2 smem_out_value(Store &store, int slot, int col
     }
 }
 
-// Runs one length-N transform per row.  All threads of the CTA must call it
-// (it synchronises the block).  `srow` is this thread's shared row.
+// Barriers of the engine: the whole CTA, or only the P threads (whole warps)
+// that transform one row, with a named barrier per row.
+struct CtaSync {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+struct RowSync {
+    int id;      // 1..15 (0 is the CTA barrier)
+    int count;   // threads of the row, a multiple of 32
+    __device__ __forceinline__ void operator()() const {
+        asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+    }
+};
+
+// Runs one length-N transform per row.  Every thread that `sync` covers must
+// call it.  `srow` is this thread's shared row.
 //
 //   Load:  float2 load(int slot, int col)   -- slot = m*R0 + r (compile-time after unrolling)
 //   Store: void store(int slot, int col, float2 v)
 //   OUT_SMEM: write the outputs to srow (after an internal barrier) and call
 //             store() first so it may transform the value; ends with a barrier.
 //             store() must then RETURN the value to write: float2 store(slot, col, v).
-template <int N, int E, bool INV, bool OUT_SMEM = false, class Load, class Store>
-__device__ __forceinline__ void fft_row(float2 *__restrict__ srow, int j, const float2 *__restrict__ tw,
-                                        Load &&load, Store &&store) {
+template <int N, int E, bool INV, bool OUT_SMEM = false, class Load, class Store, class Sync>
+__device__ __forceinline__ void fft_row_sync(float2 *__restrict__ srow, int j, const float2 *__restrict__ tw,
+                                             Load &&load, Store &&store, const Sync &sync) {
     using PL = FftPlan<N, E>;
     constexpr int P = PL::P;
     float2 v[E];
@@ -106,9 +119,9 @@ __device__ __forceinline__ void fft_row(float2 *__restrict__ srow, int j, const 
         // N == 1: identity transform.
         v[0] = load(0, 0);
         if constexpr (OUT_SMEM) {
-            __syncthreads();
+            sync();
             srow[0] = store(0, 0, v[0]);
-            __syncthreads();
+            sync();
         } else {
             store(0, 0, v[0]);
         }
@@ -163,7 +176,7 @@ __device__ __forceinline__ void fft_row(float2 *__restrict__ srow, int j, const 
                     for (int r = 0; r < R; ++r) store(m * R + r, b + r * NS, v[m * R + r]);
                 }
             } else {
-                __syncthreads();   // every thread has read this stage's inputs
+                sync();   // every thread has read this stage's inputs
 #pragma unroll
                 for (int m = 0; m < M; ++m) {
                     const int b = j + m * P;
@@ -178,10 +191,17 @@ __device__ __forceinline__ void fft_row(float2 *__restrict__ srow, int j, const 
                         }
                     }
                 }
-                __syncthreads();
+                sync();
             }
         });
     }
+}
+
+// The transform with CTA-wide barriers.
+template <int N, int E, bool INV, bool OUT_SMEM = false, class Load, class Store>
+__device__ __forceinline__ void fft_row(float2 *__restrict__ srow, int j, const float2 *__restrict__ tw,
+                                        Load &&load, Store &&store) {
+    fft_row_sync<N, E, INV, OUT_SMEM>(srow, j, tw, load, store, CtaSync{});
 }
 
 // Column of output slot `slot` (= m*R + r of the last stage) for thread j.

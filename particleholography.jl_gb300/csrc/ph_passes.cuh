@@ -16,14 +16,18 @@
 // once and transforms several slices from them; pass B double-buffers the rows
 // of the next slice while it transforms the current one.
 //
-// Each pass chooses its elements per thread (EPT, the main radix) and the CTAs
-// per SM it asks the register allocator for (MINB): fewer values per thread
-// buy more resident warps where the pass is latency-bound.
+// Each pass chooses its elements per thread (EPT, the main radix), its CTA size
+// (TT) and the resident threads per SM its register budget is sized for (RTS):
+// more resident warps hide more latency where a pass is latency-bound.
 #pragma once
 
 #include <cuda_fp16.h>
 #include "ph_fft.cuh"
 #include "ph_tma.cuh"
+
+#ifndef PH_RECONB_RTS
+#define PH_RECONB_RTS 640
+#endif
 
 namespace ph {
 
@@ -55,12 +59,13 @@ struct ThreadMap {
 
 constexpr size_t kSmemMax = 227 * 1024;   // opt-in dynamic shared memory per CTA
 
-// Defaults of a pass: radix-16 engine, one CTA per SM of register budget, one
-// padded exchange row per transformed row of shared memory.
+// Defaults of a pass: radix-16 engine, 512-thread CTAs, registers for 512
+// resident threads per SM (128 per thread), one padded exchange row per
+// transformed row of shared memory.
 struct PassBase {
     static constexpr int EPT = 16;
     static constexpr int TT = 512;    // target threads per CTA
-    static constexpr int MINB = 1;
+    static constexpr int RTS = 512;   // resident threads per SM the register budget allows
     template <int N, bool ROW_FAST>
     static constexpr size_t smem() { return Shape<N, EPT, TT>::template smem_bytes<ROW_FAST>(); }
 };
@@ -70,10 +75,10 @@ __device__ __forceinline__ float2 *xrow(unsigned char *base, int r) {
     return reinterpret_cast<float2 *>(base) + (size_t)r * Shape<N, EPT, TT>::template stride<ROW_FAST>();
 }
 
-// Register budget: MINB x 512 resident threads per SM.
+// Register budget: RTS resident threads per SM.
 template <int N, class Body>
 constexpr int min_blocks() {
-    return cmax(1, Body::MINB * 512 / Shape<N, Body::EPT, Body::TT>::THREADS);
+    return cmax(1, Body::RTS / Shape<N, Body::EPT, Body::TT>::THREADS);
 }
 
 template <int N, bool ROW_FAST, class Body>
@@ -200,11 +205,11 @@ struct ReconA : PassBase {
         constexpr size_t dense = (size_t)N * 16;
         return (dense + 127) / 128 * 128 + (16 * (8 / (R < 8 ? R : 8))) % 128;
     }
-    // Staged when MINB CTAs with their state rows and exchange rows fit an SM.
+    // Staged when the state rows and the exchange rows fit the CTA's shared memory.
     template <int N, bool RF>
     static constexpr bool staged() {
-        return MINB * ((size_t)Shape<N, EPT, TT>::ROWS * state_stride<N>() + Shape<N, EPT, TT>::template smem_bytes<RF>() +
-                       16) <= kSmemMax;
+        return (size_t)Shape<N, EPT, TT>::ROWS * state_stride<N>() + Shape<N, EPT, TT>::template smem_bytes<RF>() +
+                   16 <= kSmemMax;
     }
     template <int N, bool RF>
     static constexpr size_t stage_total() {
@@ -222,7 +227,11 @@ struct ReconA : PassBase {
         constexpr size_t SS = state_stride<N>();
         unsigned char *xbase = smem + stage_total<N, RF>();
         uint64_t *bar = reinterpret_cast<uint64_t *>(xbase + S::template smem_bytes<RF>());
-        const int kx0 = blockIdx.x * ROWS;
+        // The CTAs of one row block (its `gridDim.y` slice groups) are consecutive
+        // in launch order, so they run together and share its state rows in L2.
+        const int lin = blockIdx.y * gridDim.x + blockIdx.x;
+        const int g = lin % gridDim.y;
+        const int kx0 = (lin / gridDim.y) * ROWS;
         const int kx = kx0 + r;
         const bool valid = kx < nx;
         const float4 *srow;
@@ -244,7 +253,7 @@ struct ReconA : PassBase {
             srow = state + (size_t)(valid ? kx : 0) * N;
         }
         float2 *xr = xrow<N, EPT, TT, RF>(xbase, r);
-        const int b0 = blockIdx.y * group;
+        const int b0 = g * group;
         const int b1 = min(b0 + group, nbatch);
         for (int b = b0; b < b1; ++b) {
             const uint32_t k = (uint32_t)(k0 + b);
@@ -285,13 +294,15 @@ __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f),
 // ROWS rows for `group` consecutive batch slots; with EPI_PROJ the running
 // minimum stays in registers across them and is merged with one atomicMin of
 // (float bits << 32 | slice) per pixel.  The rows of slice b+1 arrive in
-// shared memory by bulk copy while slice b is transformed (two buffers).
-// CTAs are small (128 threads: one row at N >= 2048) so that the barriers of
-// the FFT stages span only the warps that exchange data, and four CTAs share
-// an SM.
+// shared memory by bulk copy while slice b is transformed: two buffers, each
+// first the bulk-copy target (dense rows) and then, after the first stage has
+// read it, the exchange rows of that slice's transform.  CTAs are small (128
+// threads: one row at N >= 2048) so that the barriers of the FFT stages span
+// only the warps that exchange data, and RTS / 128 CTAs share an SM.
 template <int EPI>
 struct ReconB : PassBase {
-    static constexpr int TT = 128;   // one row per CTA at N >= 2048: barriers span one row's warps
+    static constexpr int TT = 128;
+    static constexpr int RTS = PH_RECONB_RTS;
     const float2 *t;                 // [batch][rows][nx]
     const float2 *tw;
     unsigned long long *proj64;      // [rows_out][nx_out] or null
@@ -303,18 +314,20 @@ struct ReconB : PassBase {
     int k0, nbatch, group;
     long long vol_slice_stride;      // elements per stored slice
 
+    // One buffer: the exchange rows (which also hold the dense bulk-copied rows).
+    template <int N, bool RF>
+    static constexpr size_t buf_bytes() {
+        return (Shape<N, EPT, TT>::template smem_bytes<RF>() + 127) / 128 * 128;
+    }
     // Staged when a row is a multiple of 16 bytes (bulk-copy granularity) and
-    // MINB CTAs with two stage buffers plus the exchange rows fit an SM.
+    // two buffers fit the CTA's shared memory.
     template <int N, bool RF>
     static constexpr bool staged() {
-        return N % 2 == 0 && MINB * (2 * (size_t)Shape<N, EPT, TT>::ROWS * N * 8 +
-                                     Shape<N, EPT, TT>::template smem_bytes<RF>() + 16) <= kSmemMax;
+        return N % 2 == 0 && 2 * buf_bytes<N, RF>() + 16 <= kSmemMax;
     }
     template <int N, bool RF>
-    static constexpr size_t stage_bytes() { return staged<N, RF>() ? (size_t)Shape<N, EPT, TT>::ROWS * N * 8 : 0; }
-    template <int N, bool RF>
     static constexpr size_t smem() {
-        return 2 * stage_bytes<N, RF>() + Shape<N, EPT, TT>::template smem_bytes<RF>() + 16;
+        return staged<N, RF>() ? 2 * buf_bytes<N, RF>() + 16 : Shape<N, EPT, TT>::template smem_bytes<RF>();
     }
 
     template <int N, bool RF>
@@ -322,10 +335,8 @@ struct ReconB : PassBase {
         using S = Shape<N, EPT, TT>;
         constexpr int E = S::E;
         constexpr int ROWS = S::ROWS;
-        constexpr size_t SB = stage_bytes<N, RF>();
-        unsigned char *xbase = smem + 2 * SB;
-        uint64_t *bars = reinterpret_cast<uint64_t *>(xbase + S::template smem_bytes<RF>());
-        float2 *xr = xrow<N, EPT, TT, RF>(xbase, r);
+        constexpr size_t BB = buf_bytes<N, RF>();
+        uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * BB);
         const int yb = blockIdx.x * ROWS;
         const int y = yb + r;
         const bool valid = y < rows;
@@ -336,7 +347,7 @@ struct ReconB : PassBase {
             fence_proxy_async_smem();
             mbar_arrive_expect_tx(bars + buf, (uint32_t)(nvalid * N * 8));
             for (int q = 0; q < nvalid; ++q)
-                bulk_g2s(smem + buf * SB + (size_t)q * N * 8, t + ((size_t)b * rows + yb + q) * N, N * 8, bars + buf);
+                bulk_g2s(smem + buf * BB + (size_t)q * N * 8, t + ((size_t)b * rows + yb + q) * N, N * 8, bars + buf);
         };
         if constexpr (staged<N, RF>()) {
             if (threadIdx.x == 0) {
@@ -359,14 +370,18 @@ struct ReconB : PassBase {
             const int k = k0 + b;
             const int buf = (b - b0) & 1;
             const float2 *in;
+            float2 *xr;
             if constexpr (staged<N, RF>()) {
-                // the other buffer was last read before this iteration's barriers: refill it
+                // every thread is done with the other buffer (slice b-1's last stage): refill it
+                __syncthreads();
                 if (threadIdx.x == 0 && b + 1 < b1) issue(b + 1, buf ^ 1);
                 mbar_wait(bars + buf, (parity >> buf) & 1u, err);
                 parity ^= 1u << buf;
-                in = reinterpret_cast<const float2 *>(smem + buf * SB) + (size_t)r * N;
+                in = reinterpret_cast<const float2 *>(smem + buf * BB) + (size_t)r * N;
+                xr = xrow<N, EPT, TT, RF>(smem + buf * BB, r);
             } else {
                 in = t + ((size_t)b * rows + (valid ? y : 0)) * N;
+                xr = xrow<N, EPT, TT, RF>(smem, r);
             }
             fft_row<N, E, true>(
                 xr, j, tw, [&](int, int kx) -> float2 { return in[kx]; },
