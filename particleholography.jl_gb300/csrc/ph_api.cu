@@ -178,6 +178,26 @@ __global__ void k_resid_finish(const double *acc, double *out) {
     *out = acc[1] > 0.0 ? sqrt(acc[0] / acc[1]) : 0.0;
 }
 
+// ht[kx][ky] = scale * h[shift(ky)][shift(kx)]: a centred [ny][nx] transfer
+// rearranged to the [kx][ky] rows the staged column pass multiplies by
+// (32 x 32 tiles through shared memory, both sides coalesced).
+__global__ void k_transfer_rows(float2 *ht, const float2 *h, int nx, int ny, float scale) {
+    __shared__ float2 tile[32][33];
+    const int kx0 = blockIdx.x * 32, ky0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int ky = ky0 + i, kx = kx0 + threadIdx.x;
+        if (ky < ny && kx < nx) tile[i][threadIdx.x] = h[(size_t)shift_idx(ky, ny) * nx + shift_idx(kx, nx)];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int kx = kx0 + i, ky = ky0 + threadIdx.x;
+        if (kx < nx && ky < ny) {
+            const float2 v = tile[threadIdx.x][i];
+            ht[(size_t)kx * ny + ky] = make_float2(v.x * scale, v.y * scale);
+        }
+    }
+}
+
 // ---------------------------------------------------------------- call plumbing
 
 void set_err(ph_ctx *ctx, const char *fmt, ...) {
@@ -860,10 +880,15 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
         if (residual) PH_CUDA(cudaMemsetAsync(residual, 0, sizeof(double), s), "memset");
         PH_LEAVE(ctx);
     }
+    // The staged persistent passes take the transfers as [kx][ky] rows.
+    const bool staged = gs_row_staged(nx) && gs_col_staged(ny);
     Arena a;
     const size_t oa = a.take<float2>(n), ob = a.take<float2>(n);
+    const size_t oh = staged ? a.take<float2>(n) : 0, ohi = staged ? a.take<float2>(n) : 0;
     PH_TRY(ensure_scratch(ctx, a.off, s));
     float2 *bufa = at<float2>(ctx, oa), *bufb = at<float2>(ctx, ob);
+    float2 *ht = staged ? at<float2>(ctx, oh) : nullptr, *hti = staged ? at<float2>(ctx, ohi) : nullptr;
+    int *err = static_cast<int *>(ctx->small);
     const float2 *tw_x = nullptr, *tw_y = nullptr;
     PH_TRY(get_twiddles(ctx, nx, s, &tw_x));
     PH_TRY(get_twiddles(ctx, ny, s, &tw_y));
@@ -872,6 +897,13 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
              (const void *)holo2, transfer, invtransfer, (void *)residual, ctx->scratch);
     PH_TRY(run_graph(ctx, s, key, [&](cudaStream_t s) -> int {
     if (residual) PH_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s), "memset");
+    const float scale = (float)(1.0 / ((double)nx * (double)ny));
+    if (staged) {
+        dim3 tb(32, 8), tg((nx + 31) / 32, (ny + 31) / 32);
+        k_transfer_rows<<<tg, tb, 0, s>>>(ht, static_cast<const float2 *>(transfer), nx, ny, scale);
+        k_transfer_rows<<<tg, tb, 0, s>>>(hti, static_cast<const float2 *>(invtransfer), nx, ny, scale);
+        PH_TRY(launched(ctx, cudaGetLastError(), "transfer rows", 2));
+    }
 
     FwdRowsT<FWD_SQRT_REAL> f{};
     f.src_real = holo1;
@@ -879,8 +911,28 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
     f.tw = tw_x;
     f.nrows = ny;
     PH_TRY(pass(ctx, s, "fwd_rows",[&] { return launch_fwd_rows(nx, f, s); }));
-    const float scale = (float)(1.0 / ((double)nx * (double)ny));
-    for (int it = 0; it < priter; ++it) {
+    for (int it = 0; it < priter && staged; ++it) {
+        const bool last = it == priter - 1;
+        GsColT c{};
+        c.src = bufa; c.ht = ht; c.dst = bufb; c.tw = tw_y; c.err = err; c.nx = nx;
+        PH_TRY(pass(ctx, s, "gs_col",[&] { return launch_gs_col_t(ny, c, s); }));
+        GsRowMidT r2{};
+        r2.src = bufb; r2.holo = holo2; r2.dst = bufa; r2.tw = tw_x; r2.err = err; r2.nrows = ny;
+        r2.resid = (last && residual) ? acc : nullptr;
+        PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return launch_gs_row_t(nx, r2, s); }));
+        c.src = bufa; c.ht = hti; c.dst = bufb;
+        PH_TRY(pass(ctx, s, "gs_col",[&] { return launch_gs_col_t(ny, c, s); }));
+        if (!last) {
+            GsRowMidT r1{};
+            r1.src = bufb; r1.holo = holo1; r1.dst = bufa; r1.tw = tw_x; r1.err = err; r1.nrows = ny;
+            PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return launch_gs_row_t(nx, r1, s); }));
+        } else {
+            GsRow<ROW_FINAL> r1{};
+            r1.src = bufb; r1.holo = holo1; r1.dst = o; r1.tw = tw_x; r1.nrows = ny;
+            PH_TRY(pass(ctx, s, "gs_row_final",[&] { return launch_gs_row(nx, r1, s); }));
+        }
+    }
+    for (int it = 0; it < priter && !staged; ++it) {
         const bool last = it == priter - 1;
         GsCol c{};
         c.src = bufa; c.h = static_cast<const float2 *>(transfer); c.dst = bufb; c.tw = tw_y; c.nx = nx;

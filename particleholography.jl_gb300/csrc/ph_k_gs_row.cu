@@ -13,4 +13,10 @@ cudaError_t launch_gs_row(int n, const GsRow<ROW_INV> &b, cudaStream_t s) {
     return launch_len<false>(n, b, b.nrows, 1, s);
 }
 
+cudaError_t launch_gs_row_t(int n, const GsRowMidT &b, cudaStream_t s) {
+    return launch_staged_len<true>(n, b, b.nrows, s);
+}
+
+bool gs_row_staged(int n) { return staged_len<GsRowMidT>(n); }
+
 }  // namespace ph

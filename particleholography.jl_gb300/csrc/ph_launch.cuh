@@ -45,9 +45,52 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) 
         }
     }
     using S = Shape<N, Body::EPT, Body::TT>;
-    dim3 grid((nrows + S::ROWS - 1) / S::ROWS, grid_y);
+    int gx = (nrows + S::ROWS - 1) / S::ROWS;
+    if constexpr (Body::template persistent<N>()) {
+        // one CTA per resident slot (per device: the occupancy of this kernel x SMs)
+        static int slots[64] = {};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        int c = __atomic_load_n(&slots[dev & 63], __ATOMIC_ACQUIRE);
+        if (c == 0) {
+            int per_sm = 0, sms = 0;
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::THREADS, smem);
+            if (e != cudaSuccess) return e;
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
+            c = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+            __atomic_store_n(&slots[dev & 63], c, __ATOMIC_RELEASE);
+        }
+        gx = gx < c ? gx : c;
+    }
+    if (gx == 0) return cudaSuccess;
+    dim3 grid(gx, grid_y);
     kern<<<grid, S::THREADS, smem, s>>>(body);
     return cudaGetLastError();
+}
+
+// Launch of a pass that exists only for the lengths where Body::staged<N>() holds.
+template <bool ROW_FAST, class Body>
+cudaError_t launch_staged_len(int n, const Body &body, int nrows, cudaStream_t s) {
+    switch (n) {
+#define PH_STAGED_CASE(N)                                                             \
+    case N:                                                                          \
+        if constexpr (Body::template staged<N>()) return launch_one<N, ROW_FAST>(body, nrows, 1, s); \
+        else return cudaErrorInvalidValue;
+        PH_FOR_EACH_N(PH_STAGED_CASE)
+#undef PH_STAGED_CASE
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <class Body>
+bool staged_len(int n) {
+    switch (n) {
+#define PH_STAGED_Q(N) case N: return Body::template staged<N>();
+        PH_FOR_EACH_N(PH_STAGED_Q)
+#undef PH_STAGED_Q
+    }
+    return false;
 }
 
 template <bool ROW_FAST, class Body>
@@ -74,5 +117,10 @@ cudaError_t launch_gs_row(int n, const GsRow<ROW_MID> &b, cudaStream_t s);
 cudaError_t launch_gs_row(int n, const GsRow<ROW_FINAL> &b, cudaStream_t s);
 cudaError_t launch_gs_row(int n, const GsRow<ROW_INV> &b, cudaStream_t s);
 cudaError_t launch_gs_col(int n, const GsCol &b, cudaStream_t s);
+// Persistent staged GS passes (row lengths where gs_row_staged / gs_col_staged hold).
+bool gs_row_staged(int n);
+bool gs_col_staged(int n);
+cudaError_t launch_gs_row_t(int n, const GsRowMidT &b, cudaStream_t s);
+cudaError_t launch_gs_col_t(int n, const GsColT &b, cudaStream_t s);
 
 }  // namespace ph

@@ -25,6 +25,9 @@
 #include "ph_fft.cuh"
 #include "ph_tma.cuh"
 
+#ifndef PH_HT_EARLY
+#define PH_HT_EARLY 1
+#endif
 #ifndef PH_RECONB_RTS
 #define PH_RECONB_RTS 640
 #endif
@@ -68,7 +71,20 @@ struct PassBase {
     static constexpr int RTS = 512;   // resident threads per SM the register budget allows
     template <int N, bool ROW_FAST>
     static constexpr size_t smem() { return Shape<N, EPT, TT>::template smem_bytes<ROW_FAST>(); }
+    // Persistent passes loop over row blocks; their grid is the resident CTA count.
+    template <int N>
+    static constexpr bool persistent() { return false; }
 };
+
+constexpr size_t round128(size_t b) { return (b + 127) / 128 * 128; }
+
+// The pointer, hidden from the optimiser: loads through it are not hoisted
+// out of the enclosing loop (which would pin the values in registers).
+template <class T>
+__device__ __forceinline__ T *opaque(T *p) {
+    asm volatile("" : "+l"(p));
+    return p;
+}
 
 template <int N, int EPT, int TT, bool ROW_FAST>
 __device__ __forceinline__ float2 *xrow(unsigned char *base, int r) {
@@ -544,6 +560,213 @@ struct GsCol : PassBase {
             [&](int, int y, float2 v) {
                 if (valid) dst[(size_t)y * nx + kx] = v;
             });
+    }
+};
+
+// ---------------------------------------------------------------- staged Gerchberg-Saxton passes
+
+// Row stride (elements) of a staged row of ROWS rows read rows-fastest across
+// lanes: a multiple of 16 bytes, with consecutive rows 16/ROWS 8-byte words (or
+// 32/ROWS 4-byte words) apart, so that the ROWS x (16/ROWS) lanes of an access
+// phase fall on distinct banks.
+template <int N, int ROWS, int ELEM>
+constexpr int staged_stride() {
+    return ELEM == 8 ? (N + 15) / 16 * 16 + (16 / ROWS) % 16 : (N + 31) / 32 * 32 + (32 / ROWS) % 32;
+}
+
+// Persistent form of the GS row pass with the transposed store (ROW_MID): each
+// CTA walks row blocks rb = blockIdx.x, blockIdx.x + gridDim.x, ...; the field
+// rows and hologram rows of the next block arrive by bulk copy into the second
+// of two buffers while the current block is transformed.  A field buffer holds
+// the dense rows at the exchange-row offsets, so the transform runs in place.
+struct GsRowMidT : PassBase {
+    const float2 *src;       // [ny][nx]
+    const float *holo;       // [ny][nx]
+    float2 *dst;             // [nx][ny]
+    const float2 *tw;
+    double *resid;           // nullable: [0] += (|u| - s)^2, [1] += s^2
+    int *err;                // raised if a bulk-copy wait times out
+    int nrows;
+
+    template <int N>
+    using S = Shape<N, EPT, TT>;
+    template <int N>
+    static constexpr size_t fbytes() { return round128(S<N>::template smem_bytes<true>()); }
+    template <int N>
+    static constexpr size_t hbytes() { return round128((size_t)S<N>::ROWS * staged_stride<N, S<N>::ROWS, 4>() * 4); }
+    template <int N>
+    static constexpr size_t buf_bytes() { return fbytes<N>() + hbytes<N>(); }
+    template <int N>
+    static constexpr bool staged() {
+        return S<N>::ROWS <= 8 && N % 4 == 0 && 2 * buf_bytes<N>() + 16 <= kSmemMax;
+    }
+    template <int N>
+    static constexpr bool persistent() { return true; }
+    template <int N, bool RF>
+    static constexpr size_t smem() { return 2 * buf_bytes<N>() + 16; }
+
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
+        static_assert(RF, "rows-fastest launch");
+        using SN = S<N>;
+        constexpr int E = SN::E, ROWS = SN::ROWS;
+        constexpr int FS = SN::template stride<true>();
+        constexpr int HS = staged_stride<N, ROWS, 4>();
+        constexpr size_t FB = fbytes<N>(), BUF = buf_bytes<N>();
+        uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * BUF);
+        const int nblocks = (nrows + ROWS - 1) / ROWS;
+        auto issue = [&](int rb, int buf) {   // one thread: field and hologram rows of block rb
+            const int yb = rb * ROWS, nv = min(ROWS, nrows - yb);
+            unsigned char *base = smem + buf * BUF;
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(bars + buf, (uint32_t)(nv * N * 12));
+            for (int q = 0; q < nv; ++q) {
+                bulk_g2s(base + (size_t)q * FS * 8, src + (size_t)(yb + q) * N, N * 8, bars + buf);
+                bulk_g2s(base + FB + (size_t)q * HS * 4, holo + (size_t)(yb + q) * N, N * 4, bars + buf);
+            }
+        };
+        if (threadIdx.x == 0) {
+            mbar_init(bars, 1);
+            mbar_init(bars + 1, 1);
+            mbar_fence_init();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && (int)blockIdx.x < nblocks) issue(blockIdx.x, 0);
+        uint32_t parity = 0;
+        double acc0 = 0.0, acc1 = 0.0;
+        int it = 0;
+        for (int rb = blockIdx.x; rb < nblocks; rb += gridDim.x, ++it) {
+            const int buf = it & 1;
+            __syncthreads();   // every thread is done with the other buffer
+            if (threadIdx.x == 0 && rb + (int)gridDim.x < nblocks) issue(rb + gridDim.x, buf ^ 1);
+            mbar_wait(bars + buf, (parity >> buf) & 1u, err);
+            parity ^= 1u << buf;
+            unsigned char *base = smem + buf * BUF;
+            float2 *xr = reinterpret_cast<float2 *>(base) + (size_t)r * FS;
+            const float *hr = reinterpret_cast<const float *>(base + FB) + (size_t)r * HS;
+            const int y = rb * ROWS + r;
+            const bool valid = y < nrows;
+            fft_row<N, E, true, true>(xr, j, tw, [&](int, int x) -> float2 { return xr[x]; },
+                                      [&](int, int x, float2 v) -> float2 {
+                                          const float s = sqrtf(hr[x]);
+                                          if (resid != nullptr && valid) {
+                                              const double a = sqrt((double)v.x * v.x + (double)v.y * v.y) - (double)s;
+                                              acc0 += a * a;
+                                              acc1 += (double)s * s;
+                                          }
+                                          return amplitude_replace(v, s);
+                                      });
+            fft_row<N, E, false>(xr, j, tw, [&](int, int x) -> float2 { return xr[spad(x)]; },
+                                 [&](int, int kx, float2 v) {
+                                     if (valid) dst[(size_t)kx * nrows + y] = v;
+                                 });
+        }
+        if (resid != nullptr) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
+                acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
+            }
+            if ((threadIdx.x & 31) == 0) {
+                atomicAdd(resid, acc0);
+                atomicAdd(resid + 1, acc1);
+            }
+        }
+    }
+};
+
+// Persistent form of the GS column pass: rows kx of [kx][y] data, forward FFT
+// along y, times ht[kx][ky] (the centred transfer rearranged to this layout,
+// scale included), inverse FFT along y, transposed store [y][kx].  The field
+// rows are double-buffered; the transfer rows of the next block are copied in
+// once this block's multiply has read them.
+struct GsColT : PassBase {
+    static constexpr bool HT_EARLY = PH_HT_EARLY;
+    const float2 *src;       // [nx][ny]
+    const float2 *ht;        // [nx][ny]
+    float2 *dst;             // [ny][nx]
+    const float2 *tw;
+    int *err;
+    int nx;
+
+    template <int N>
+    using S = Shape<N, EPT, TT>;
+    template <int N>
+    static constexpr size_t fbytes() { return round128(S<N>::template smem_bytes<true>()); }
+    template <int N>
+    static constexpr size_t hbytes() { return round128((size_t)S<N>::ROWS * staged_stride<N, S<N>::ROWS, 8>() * 8); }
+    template <int N>
+    static constexpr bool staged() {
+        return S<N>::ROWS <= 8 && N % 2 == 0 && 2 * fbytes<N>() + hbytes<N>() + 32 <= kSmemMax;
+    }
+    template <int N>
+    static constexpr bool persistent() { return true; }
+    template <int N, bool RF>
+    static constexpr size_t smem() { return 2 * fbytes<N>() + hbytes<N>() + 32; }
+
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
+        static_assert(RF, "rows-fastest launch");
+        using SN = S<N>;
+        constexpr int E = SN::E, ROWS = SN::ROWS;
+        constexpr int FS = SN::template stride<true>();
+        constexpr int HS = staged_stride<N, ROWS, 8>();
+        constexpr size_t FB = fbytes<N>(), HB = hbytes<N>();
+        unsigned char *hbase = smem + 2 * FB;
+        uint64_t *bars = reinterpret_cast<uint64_t *>(hbase + HB);   // [0], [1] field buffers, [2] transfer
+        const int nblocks = (nx + ROWS - 1) / ROWS;
+        auto issue_field = [&](int rb, int buf) {
+            const int kb = rb * ROWS, nv = min(ROWS, nx - kb);
+            unsigned char *base = smem + buf * FB;
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(bars + buf, (uint32_t)(nv * N * 8));
+            for (int q = 0; q < nv; ++q)
+                bulk_g2s(base + (size_t)q * FS * 8, src + (size_t)(kb + q) * N, N * 8, bars + buf);
+        };
+        auto issue_ht = [&](int rb) {
+            const int kb = rb * ROWS, nv = min(ROWS, nx - kb);
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(bars + 2, (uint32_t)(nv * N * 8));
+            for (int q = 0; q < nv; ++q)
+                bulk_g2s(hbase + (size_t)q * HS * 8, ht + (size_t)(kb + q) * N, N * 8, bars + 2);
+        };
+        if (threadIdx.x == 0) {
+            mbar_init(bars, 1);
+            mbar_init(bars + 1, 1);
+            mbar_init(bars + 2, 1);
+            mbar_fence_init();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && (int)blockIdx.x < nblocks) {
+            issue_field(blockIdx.x, 0);
+            issue_ht(blockIdx.x);
+        }
+        uint32_t parity = 0;   // bits 0, 1: field buffers; bit 2: transfer buffer
+        int it = 0;
+        for (int rb = blockIdx.x; rb < nblocks; rb += gridDim.x, ++it) {
+            const int buf = it & 1;
+            const int next = rb + gridDim.x;
+            __syncthreads();   // every thread is done with the other field buffer
+            if (threadIdx.x == 0 && next < nblocks) issue_field(next, buf ^ 1);
+            if (!HT_EARLY && threadIdx.x == 0 && it > 0) issue_ht(rb);
+            mbar_wait(bars + buf, (parity >> buf) & 1u, err);
+            parity ^= 1u << buf;
+            mbar_wait(bars + 2, (parity >> 2) & 1u, err);
+            parity ^= 4u;
+            float2 *xr = reinterpret_cast<float2 *>(smem + buf * FB) + (size_t)r * FS;
+            const float2 *hr = reinterpret_cast<const float2 *>(hbase) + (size_t)r * HS;
+            const int kx = rb * ROWS + r;
+            const bool valid = kx < nx;
+            const float2 *tw = opaque(this->tw);   // twiddles are re-read per block, not held in registers
+            fft_row<N, E, false, true>(xr, j, tw, [&](int, int y) -> float2 { return xr[y]; },
+                                       [&](int, int ky, float2 v) -> float2 { return cmul(v, hr[ky]); });
+            // the transform ended with a barrier: the transfer rows are free
+            if (HT_EARLY && threadIdx.x == 0 && next < nblocks) issue_ht(next);
+            fft_row<N, E, true>(xr, j, tw, [&](int, int ky) -> float2 { return xr[spad(ky)]; },
+                                [&](int, int y, float2 v) {
+                                    if (valid) dst[(size_t)y * nx + kx] = v;
+                                });
+        }
     }
 };
 
