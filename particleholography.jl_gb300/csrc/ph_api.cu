@@ -44,12 +44,25 @@ constexpr int kMaxGraphs = 32;
 
 // ---------------------------------------------------------------- setup kernels
 
+__device__ __forceinline__ float2 twiddle_fp64(int i, int n) {   // W_n^i rounded from FP64
+    double s, c;
+    sincospi(-2.0 * (double)i / (double)n, &s, &c);
+    return make_float2((float)c, (float)s);
+}
+
 __global__ void k_twiddle(float2 *tw, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    double s, c;
-    sincospi(-2.0 * (double)i / (double)n, &s, &c);
-    tw[i] = make_float2((float)c, (float)s);
+    tw[i] = twiddle_fp64(i, n);
+}
+
+// The stage blocks of the table (layout in ph_fft.cuh): entry [r-1][k] of the
+// block of a stage with radix R and span NS is W_n^(r k n / (NS R)).
+__global__ void k_twiddle_stage(float2 *blk, int n, int radix, int ns) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (radix - 1) * ns) return;
+    const int r = e / ns + 1, k = e % ns;
+    blk[e] = twiddle_fp64(r * k * (n / (ns * radix)), n);
 }
 
 // holofunc.jl:8-15 with the reference's Float64 operation order; the
@@ -326,10 +339,18 @@ int get_twiddles(ph_ctx *ctx, int n, cudaStream_t s, const float2 **out) {
         return PH_ERR_INVALID;
     }
     float2 *p = nullptr;
-    PH_CUDA(cudaMalloc(&p, sizeof(float2) * (size_t)n), "cudaMalloc(twiddles)");
+    const int e = engine_e(n, PassBase::EPT);
+    PH_CUDA(cudaMalloc(&p, sizeof(float2) * (size_t)plan_tw_size(n, e)), "cudaMalloc(twiddles)");
     k_twiddle<<<(n + 255) / 256, 256, 0, s>>>(p, n);
     ctx->launches++;
     PH_CUDA(cudaGetLastError(), "k_twiddle");
+    for (int st = 1; st < plan_nstages(n, e); ++st) {
+        const int r = plan_radix(n, e, st), ns = plan_ns(n, e, st);
+        const int cnt = (r - 1) * ns;
+        k_twiddle_stage<<<(cnt + 255) / 256, 256, 0, s>>>(p + plan_tw_offset(n, e, st), n, r, ns);
+        ctx->launches++;
+        PH_CUDA(cudaGetLastError(), "k_twiddle_stage");
+    }
     ctx->tw[n] = p;
     *out = p;
     return PH_OK;

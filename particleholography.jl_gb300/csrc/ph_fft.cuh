@@ -27,30 +27,54 @@ namespace ph {
 // of two (radix-E stages, then a smaller power-of-two radix) or three times a
 // power of two (E = 3 E2: radix-E2 stages, a smaller power-of-two radix, and a
 // final radix-3 stage, so every stage before the last has a power-of-two
-// span).  Every radix divides E.
+// span).  Every radix divides E.  The plan is written as constexpr functions
+// of (N, E) so that the host code laying out the twiddle table follows the
+// same plan as the device engine.
+__host__ __device__ constexpr bool plan_pow2(int n) { return (n & (n - 1)) == 0; }
+__host__ __device__ constexpr int plan_r2(int n, int e) { return plan_pow2(n) ? e : e / 3; }
+__host__ __device__ constexpr int plan_nfull(int n, int e) {
+    return ilog2c(plan_r2(n, e)) == 0 ? 0 : ilog2c(plan_pow2(n) ? n : n / 3) / ilog2c(plan_r2(n, e));
+}
+__host__ __device__ constexpr int plan_last(int n, int e) {   // trailing power-of-two radix (1 = none)
+    return 1 << (ilog2c(plan_pow2(n) ? n : n / 3) - plan_nfull(n, e) * ilog2c(plan_r2(n, e)));
+}
+__host__ __device__ constexpr int plan_nstages(int n, int e) {
+    return plan_nfull(n, e) + (plan_last(n, e) > 1 ? 1 : 0) + (plan_pow2(n) ? 0 : 1);
+}
+__host__ __device__ constexpr int plan_radix(int n, int e, int s) {
+    return s < plan_nfull(n, e) ? plan_r2(n, e) : ((plan_last(n, e) > 1 && s == plan_nfull(n, e)) ? plan_last(n, e) : 3);
+}
+__host__ __device__ constexpr int plan_ns(int n, int e, int s) {   // product of the radices before stage s
+    int v = 1;
+    for (int t = 0; t < s; ++t) v *= plan_radix(n, e, t);
+    return v;
+}
+// Twiddle table layout: W_N^i for i in [0, N), then for every stage s >= 1 a
+// block of (R - 1) x NS twiddles, entry [r - 1][k] = W_N^(r k N / (NS R)).  A
+// stage's lanes (consecutive butterflies, consecutive k) read consecutive
+// entries of one block row.
+__host__ __device__ constexpr int plan_tw_offset(int n, int e, int s) {
+    int off = n;
+    for (int t = 1; t < s; ++t) off += (plan_radix(n, e, t) - 1) * plan_ns(n, e, t);
+    return off;
+}
+__host__ __device__ constexpr int plan_tw_size(int n, int e) { return plan_tw_offset(n, e, plan_nstages(n, e)); }
+
 template <int N, int E>
 struct FftPlan {
-    static constexpr bool POW2 = (N & (N - 1)) == 0;
+    static constexpr bool POW2 = plan_pow2(N);
     static_assert(N >= 1 && (POW2 || ((N % 3) == 0 && ((N / 3) & (N / 3 - 1)) == 0)), "N must be 2^a or 3*2^a");
     static_assert(E >= 1 && E <= N && N % E == 0, "E must divide N");
     static constexpr int P = N / E;                       // threads per row
-    static constexpr int NP2 = POW2 ? N : N / 3;          // power-of-two part of N
-    static constexpr int R2 = POW2 ? E : E / 3;           // main power-of-two radix
-    static constexpr int LOGN = ilog2c(NP2);
-    static constexpr int LOGE = ilog2c(R2);
-    static constexpr int NFULL = LOGE == 0 ? 0 : LOGN / LOGE;
-    static constexpr int LAST = 1 << (LOGN - NFULL * LOGE);   // trailing power-of-two radix (1 = none)
-    static constexpr int NSTAGES = NFULL + (LAST > 1 ? 1 : 0) + (POW2 ? 0 : 1);
+    static constexpr int NFULL = plan_nfull(N, E);
+    static constexpr int LAST = plan_last(N, E);
+    static constexpr int NSTAGES = plan_nstages(N, E);
     template <int S>
-    __host__ __device__ static constexpr int radix() {
-        return S < NFULL ? R2 : ((LAST > 1 && S == NFULL) ? LAST : 3);
-    }
+    __host__ __device__ static constexpr int radix() { return plan_radix(N, E, S); }
     template <int S>
-    __host__ __device__ static constexpr int ns() {   // product of the radices before stage S
-        int v = 1;
-        for (int t = 0; t < S; ++t) v *= (t < NFULL ? R2 : ((LAST > 1 && t == NFULL) ? LAST : 3));
-        return v;
-    }
+    __host__ __device__ static constexpr int ns() { return plan_ns(N, E, S); }
+    template <int S>
+    __host__ __device__ static constexpr int tw_offset() { return plan_tw_offset(N, E, S); }
 };
 
 // Shared-memory index of column i of a row: one pad element per 16 keeps the
@@ -68,8 +92,8 @@ struct SmemRow {
     static constexpr int STRIDE = ((PADDED + 15) / 16) * 16 + (JC % 16);
 };
 
-// Twiddle of stage twiddle index i for a length-N transform: W_N^i (forward) or
-// its conjugate (inverse).  `tw` holds W_N^i for i in [0, N).
+// Twiddle table entry i (layout above) for the forward transform, or its
+// conjugate for the inverse.
 template <bool INV>
 __device__ __forceinline__ float2 load_tw(const float2 *__restrict__ tw, int i) {
     float2 w = __ldg(tw + i);
@@ -159,9 +183,9 @@ __device__ __forceinline__ void fft_row_sync(float2 *__restrict__ srow, int j, c
                 for (int r = 0; r < R; ++r) t[r] = v[m * R + r];
                 if constexpr (NS > 1) {
                     const int k = b & (NS - 1);
-                    constexpr int TSTEP = N / (NS * R);
+                    constexpr int TOFF = PL::template tw_offset<S>();
 #pragma unroll
-                    for (int r = 1; r < R; ++r) t[r] = cmul(t[r], load_tw<INV>(tw, r * k * TSTEP));
+                    for (int r = 1; r < R; ++r) t[r] = cmul(t[r], load_tw<INV>(tw, TOFF + (r - 1) * NS + k));
                 }
                 dft<R, INV>(t);
 #pragma unroll

@@ -29,6 +29,7 @@ inline int rows_per_cta(int n) {
 
 template <int N, bool ROW_FAST, class Body>
 cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) {
+    static_assert(Body::EPT == PassBase::EPT, "the twiddle table is laid out for the common plan");
     auto kern = k_pass<N, ROW_FAST, Body>;
     constexpr size_t smem = Body::template smem<N, ROW_FAST>();
     static_assert(smem <= kSmemMax, "pass needs more shared memory than a CTA has");

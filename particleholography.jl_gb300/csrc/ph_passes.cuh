@@ -39,11 +39,14 @@ namespace ph {
 // Shape of a pass over rows of length N with (up to) EPT values per thread:
 // E values per thread (3 * EPT/2 for N = 3 * 2^a), P threads per row, ROWS rows
 // and THREADS = ROWS * P threads (512 for every large N) per CTA.
+__host__ __device__ constexpr int engine_e(int n, int ept) {
+    return cmin(n, plan_pow2(n) ? ept : 3 * (ept / 2));
+}
+
 template <int N, int EPT = 16, int TT = 512>
 struct Shape {
     static constexpr bool POW2 = (N & (N - 1)) == 0;
-    static constexpr int EREQ = POW2 ? EPT : 3 * (EPT / 2);
-    static constexpr int E = N < EREQ ? N : EREQ;
+    static constexpr int E = engine_e(N, EPT);
     static constexpr int P = N / E;
     static constexpr int ROWS = cmax(1, cmin(64, TT / P));
     static constexpr int THREADS = ROWS * P;
