@@ -582,6 +582,18 @@ int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void 
     });
 }
 
+// Slices one pass A / pass B CTA transforms: up to 32 (fewer staging and
+// merge steps per slice), fewer when the batch would then leave pass A with
+// less than about four CTAs per SM.
+int recon_group(int nbatch, int nx_rows_a) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+    const int blocks = std::max(1, nx_rows_a);
+    const int groups = std::max(1, (4 * sms + blocks - 1) / blocks);
+    return std::max(1, std::min(32, nbatch / groups));
+}
+
 // The slice loop of a reconstruction: pass A and pass B per batch, then the
 // projection unpacking.
 int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype, int nx,
@@ -590,9 +602,10 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
                        cudaStream_t s) {
     ReconLayout L{};
     L.batch = batch;
-    const int group = 8;
+    const int row_blocks_a = (nx + rows_per_cta(ny) - 1) / rows_per_cta(ny);
     for (int k0 = 0; k0 < slices; k0 += L.batch) {
         const int nb = std::min(L.batch, slices - k0);
+        const int group = recon_group(nb, row_blocks_a);
         ReconA a{};
         a.state = state;
         a.t = t;
