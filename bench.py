@@ -144,9 +144,10 @@ class ClockSampler:
 
 # ---------------------------------------------------------------- CPU (oracle) frame sample
 
-def cpu_frame_sample(cfg: dict, h1: np.ndarray, h2: np.ndarray, gs_iters: int, slices: int):
+def cpu_frame_sample(cfg: dict, h1: np.ndarray, h2: np.ndarray, gs_iters: int, slices: int, outputs=None):
     """Times the oracle on `gs_iters` GS iterations, `slices` slices and one labeling;
-    returns (seconds per GS iteration, seconds per slice, seconds per labeling)."""
+    returns (seconds per GS iteration, seconds per slice, seconds per labeling).
+    With a dict `outputs`, also stores the oracle's field, projection and argmin there."""
     from oracle import ccl as occl
     from oracle import ref_semantics as ref
     n = cfg["n"]
@@ -161,12 +162,90 @@ def cpu_frame_sample(cfg: dict, h1: np.ndarray, h2: np.ndarray, gs_iters: int, s
     else:
         wf = ref.gabor_wavefront(h1)
     t = time.perf_counter()
-    proj = ref.reconst_xyprojection(wf, hf, hdz, slices)
+    proj, arg = ref.reconst_xyprojection(wf, hf, hdz, slices, with_argmin=True)
     t_slice = (time.perf_counter() - t) / slices
+    if outputs is not None:
+        outputs.update(wf=wf, proj=proj, arg=arg)
     t = time.perf_counter()
     occl.connected_component_labeling((proj <= cfg["threshold"]).astype(np.float32))
     t_ccl = time.perf_counter() - t
     return t_it, t_slice, t_ccl
+
+
+def cufft_standin(cfg: dict, h1, h2, hf, hdz, hp, hpi, frames: int) -> dict:
+    """The reference's kernel sequence re-enacted with torch.fft (cuFFT) and
+    one broadcast per step, on the same device buffers: GS as holofunc.jl:100-129
+    (fft, fftshift, multiply, ifftshift, ifft, angle, polar per half iteration)
+    and the projection as holofunc.jl:248-266 (cumulative X .*= Hdz, ifftshift,
+    ifft, x*conj(x), abs, min per slice, host loop).  Not the reference: a
+    stand-in for its structure on this GPU.  Labeling is left out (< 0.1 ms)."""
+    import torch
+    n, S = cfg["n"], cfg["slices"]
+    H, Hi, Hf, Hdz = (t.reshape(n, n) for t in (hp, hpi, hf, hdz))
+    s1, s2 = torch.sqrt(h1), torch.sqrt(h2)
+    fft2, ifft2, fsh, ifsh = torch.fft.fft2, torch.fft.ifft2, torch.fft.fftshift, torch.fft.ifftshift
+
+    def frame():
+        if cfg["gs_iters"] > 0:
+            u1 = torch.complex(s1, torch.zeros_like(s1))
+            for _ in range(cfg["gs_iters"]):
+                u2 = ifft2(ifsh(fsh(fft2(u1)) * H))
+                u2 = torch.polar(s2, torch.angle(u2))
+                u1 = ifft2(ifsh(fsh(fft2(u2)) * Hi))
+                u1 = torch.polar(s1, torch.angle(u1))
+        else:
+            u1 = torch.complex(s1, torch.zeros_like(s1))
+        x = fsh(fft2(u1)) * Hf
+        proj = torch.full((n, n), float("inf"), device=h1.device)
+        for k in range(S):
+            if k > 0:
+                x = x * Hdz
+            img = ifft2(ifsh(x))
+            img = torch.abs(img * torch.conj(img)).float()
+            proj = torch.minimum(proj, img)
+        return proj
+
+    frame()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(frames):
+        frame()
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / frames
+    return {"value": round(n * n * S / (ms / 1e3) / 1e6, 2), "unit": "Mvoxel/s", "ms_per_frame": round(ms, 3),
+            "frames": frames, "dtype": "c64",
+            "what": "cuFFT stand-in of the reference's kernel sequence (torch.fft + one broadcast per step, "
+                    "per-slice host loop; GS + projection, labeling excluded), same GPU and inputs"}
+
+
+def sample_accuracy(ctx, cfg, h1, h2, hp, hpi, hf, hdz, outs, gs_iters, slices, s) -> dict:
+    """Our device path on the CPU baseline's sample (same holograms, GS
+    iterations and slices), compared with the oracle outputs of that sample."""
+    import torch
+    n = cfg["n"]
+    dev = h1.device
+    wf = torch.empty((n, n), dtype=torch.complex64, device=dev)
+    if gs_iters > 0:
+        ctx.call("ph_phase_retrieval", wf.data_ptr(), h1.data_ptr(), h2.data_ptr(), hp.data.data_ptr(),
+                 hpi.data.data_ptr(), n, n, gs_iters, None, s)
+    else:
+        ctx.call("ph_gabor_wavefront", wf.data_ptr(), h1.data_ptr(), n, n, s)
+    proj = torch.empty((n, n), dtype=torch.float32, device=dev)
+    arg = torch.empty((n, n), dtype=torch.int32, device=dev)
+    ctx.call("ph_reconst_xyproj", proj.data_ptr(), arg.data_ptr(), wf.data_ptr(), hf.data.data_ptr(),
+             hdz.data.data_ptr(), n, n, slices, s)
+    torch.cuda.synchronize()
+
+    def rel(a, b):
+        a, b = np.asarray(a, dtype=np.complex128), np.asarray(b, dtype=np.complex128)
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    return {"against": "oracle FP32 (reference semantics) on the same sample",
+            "field_rel_l2": rel(wf.cpu().numpy(), outs["wf"]),
+            "projection_rel_l2": rel(proj.cpu().numpy(), outs["proj"]),
+            "argmin_agreement": float(np.mean(arg.cpu().numpy() == outs["arg"])),
+            "tolerance": {"rel_l2": 1e-4, "argmin_agreement": 0.999}}
 
 
 def cpu_mvoxel_per_s(cfg, t_it, t_slice, t_ccl) -> float:
@@ -186,6 +265,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
+    ap.add_argument("--no-standin", action="store_true", help="skip the cuFFT stand-in of the reference sequence")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
 
@@ -325,6 +405,10 @@ def main():
                "p50_frame_ms": round(statistics.median(e_ms), 3),
                "p99_frame_ms": round(float(np.percentile(e_ms, 99)), 3), "components": int(ncomp)}
 
+    standin = None
+    if not args.no_standin:
+        standin = cufft_standin(cfg, h1, h2, hf.data, hdz.data, hp.data, hpi.data, frames=2)
+
     if rank != 0:
         if world > 1:
             dist.barrier()
@@ -356,11 +440,14 @@ def main():
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         h1n, h2n = h1.cpu().numpy(), h2.cpu().numpy()
-        t_it, t_slice, t_ccl = cpu_frame_sample(cfg, h1n, h2n, 2 if cfg["gs_iters"] else 0, 16)
+        outs = {}
+        t_it, t_slice, t_ccl = cpu_frame_sample(cfg, h1n, h2n, 2 if cfg["gs_iters"] else 0, 16, outs)
         cpu = {"value": round(cpu_mvoxel_per_s(cfg, t_it, t_slice, t_ccl), 3), "unit": "Mvoxel/s",
                "cores": len(os.sched_getaffinity(0)), "kind": "port",
                "sample": f"oracle FP32 (numpy/scipy.fft workers=all): {2 if cfg['gs_iters'] else 0} GS iterations, "
-                         f"16 slices and one labeling at {n}^2, scaled to {cfg['gs_iters']} iterations + {S} slices"}
+                         f"16 slices and one labeling at {n}^2, scaled to {cfg['gs_iters']} iterations + {S} slices",
+               "accuracy": sample_accuracy(ctx, cfg, h1, h2, hp, hpi, hf, hdz, outs, 2 if cfg["gs_iters"] else 0,
+                                           16, s)}
 
     line = {
         "metric": "reconstructed Mvoxel/s + p99 frame latency, chosen vs plain FP32 form, 1 GB300",
@@ -378,6 +465,7 @@ def main():
         "kernels": kernels,
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "cufft_standin": standin,
         "clocks": clk,
     }
     print(json.dumps(line))
