@@ -65,6 +65,22 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) 
         gx = gx < c ? gx : c;
     }
     if (gx == 0) return cudaSuccess;
+    constexpr int CS = Body::template cluster<N>();
+    if constexpr (CS > 1) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((gx + CS - 1) / CS * CS, grid_y);
+        cfg.blockDim = dim3(S::THREADS);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = CS;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, kern, body);
+    }
     dim3 grid(gx, grid_y);
     kern<<<grid, S::THREADS, smem, s>>>(body);
     return cudaGetLastError();

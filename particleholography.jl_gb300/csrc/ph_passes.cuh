@@ -77,6 +77,9 @@ struct PassBase {
     // Persistent passes loop over row blocks; their grid is the resident CTA count.
     template <int N>
     static constexpr bool persistent() { return false; }
+    // CTAs per thread-block cluster (consecutive blockIdx.x).
+    template <int N>
+    static constexpr int cluster() { return 1; }
 };
 
 constexpr size_t round128(size_t b) { return (b + 127) / 128 * 128; }
@@ -209,7 +212,18 @@ struct SpectrumCols : PassBase {
 // (one bulk copy per row) and transforms `group` consecutive slices from them.
 // The state rows are spaced so that the 16-byte loads of a phase of 8 lanes
 // (ROWS rows x 8/ROWS columns) fall on distinct banks.
+//
+// The transposed store writes 4 consecutive kx (one 32-byte sector) per y.
+// Where a CTA holds fewer than 4 rows (N >= 4096), 4 / ROWS CTAs form a
+// thread-block cluster: each leaves its transformed rows in shared memory,
+// and after a cluster barrier each stores a 1 / (4 / ROWS) share of the y
+// range for all 4 rows, reading its peers' rows through distributed shared
+// memory.  (Stores of 2 consecutive kx, 16 bytes, ran 3x slower.)
 struct ReconA : PassBase {
+    template <int N>
+    static constexpr int cluster() {
+        return Shape<N, EPT, TT>::ROWS >= 4 ? 1 : 4 / Shape<N, EPT, TT>::ROWS;
+    }
     const float4 *state;   // [nx][ny]
     float2 *t;             // [batch][ny_out][nx]
     const float2 *tw;
@@ -246,11 +260,13 @@ struct ReconA : PassBase {
         constexpr size_t SS = state_stride<N>();
         unsigned char *xbase = smem + stage_total<N, RF>();
         uint64_t *bar = reinterpret_cast<uint64_t *>(xbase + S::template smem_bytes<RF>());
+        constexpr int CS = cluster<N>();
         // The CTAs of one row block (its `gridDim.y` slice groups) are consecutive
         // in launch order, so they run together and share its state rows in L2.
+        // (In a cluster launch the members of a cluster must stay consecutive.)
         const int lin = blockIdx.y * gridDim.x + blockIdx.x;
-        const int g = lin % gridDim.y;
-        const int kx0 = (lin / gridDim.y) * ROWS;
+        const int g = CS == 1 ? lin % gridDim.y : blockIdx.y;
+        const int kx0 = (CS == 1 ? lin / gridDim.y : blockIdx.x) * ROWS;
         const int kx = kx0 + r;
         const bool valid = kx < nx;
         const float4 *srow;
@@ -261,7 +277,8 @@ struct ReconA : PassBase {
             }
             __syncthreads();
             if (threadIdx.x == 0) {
-                const int nvalid = min(ROWS, nx - kx0);
+                // (CTAs that only pad a cluster hold no valid row)
+                const int nvalid = max(0, min(ROWS, nx - kx0));
                 mbar_arrive_expect_tx(bar, (uint32_t)(nvalid * N * 16));
                 for (int q = 0; q < nvalid; ++q)
                     bulk_g2s(smem + (size_t)q * SS, state + (size_t)(kx0 + q) * N, N * 16, bar);
@@ -278,23 +295,42 @@ struct ReconA : PassBase {
             const uint32_t k = (uint32_t)(k0 + b);
             const float kf = (float)k;
             float2 *tb = t + (size_t)b * ny_out * nx;
-            fft_row<N, S::E, true>(
-                xr, j, tw,
-                [&](int, int ky) -> float2 {
-                    const float4 s = srow[ky];
-                    const int32_t tt = (int32_t)(k * __float_as_uint(s.z));
-                    const float ang = (float)tt * 1.46291807926715968e-9f;   // 2 pi / 2^32
-                    float sn, cs;
-                    __sincosf(ang, &sn, &cs);
-                    const float mag = fmaf(kf, s.w, 1.0f);
-                    const float2 g = make_float2(cs * mag, sn * mag);
-                    return cmul(make_float2(s.x, s.y), g);
-                },
-                [&](int, int y, float2 v) {
+            auto load = [&](int, int ky) -> float2 {
+                const float4 s = srow[ky];
+                const int32_t tt = (int32_t)(k * __float_as_uint(s.z));
+                const float ang = (float)tt * 1.46291807926715968e-9f;   // 2 pi / 2^32
+                float sn, cs;
+                __sincosf(ang, &sn, &cs);
+                const float mag = fmaf(kf, s.w, 1.0f);
+                const float2 g = make_float2(cs * mag, sn * mag);
+                return cmul(make_float2(s.x, s.y), g);
+            };
+            if constexpr (CS == 1) {
+                fft_row<N, S::E, true>(xr, j, tw, load, [&](int, int y, float2 v) {
                     const int yo = y - y0;
                     // streaming store: T passes through L2 once
                     if (valid && yo >= 0 && yo < ny_out) __stcs(tb + (size_t)yo * nx + kx, v);
                 });
+            } else {
+                fft_row<N, S::E, true, true>(xr, j, tw, load, [](int, int, float2 v) -> float2 { return v; });
+                cluster_sync();   // every CTA of the cluster holds its transformed rows
+                constexpr int RS = S::template stride<RF>();
+                constexpr int YS = N / CS;   // y range each CTA stores
+                const uint32_t rank = cluster_ctarank();
+                const int kxc = kx0 - (int)rank * ROWS;   // first of the cluster's 4 rows
+                const uint32_t xsh = smem_addr(xbase);
+#pragma unroll
+                for (int i = 0; i < S::E; ++i) {
+                    const int f = threadIdx.x + i * S::THREADS;
+                    const int q = f & 3;
+                    const int y = (int)rank * YS + (f >> 2);
+                    const uint32_t a = xsh + (uint32_t)(((q % ROWS) * RS + spad(y)) * 8);
+                    const float2 v = ld_cluster_f2(map_to_rank(a, (uint32_t)(q / ROWS)));
+                    const int yo = y - y0;
+                    if (kxc + q < nx && yo >= 0 && yo < ny_out) __stcs(tb + (size_t)yo * nx + kxc + q, v);
+                }
+                cluster_sync();   // the peers have read these rows before the next slice rewrites them
+            }
         }
     }
 };

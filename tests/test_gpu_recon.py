@@ -21,7 +21,7 @@ def _case(n, seed=0, z0=-1000.0, dz=-200.0, n_slow=None):
 
 
 @pytest.mark.parametrize("n,slices", [(1, 2), (2, 3), (4, 3), (8, 5), (16, 7), (32, 9), (64, 12), (128, 10),
-                                      (256, 6), (512, 4), (1024, 3)])
+                                      (256, 6), (512, 4), (1024, 3), (2048, 2), (4096, 2), (8192, 2)])
 def test_xyprojection_matches_oracle(ph, cuda, n, slices):
     holo, hf, hdz = _case(n, seed=n)
     wf = ph.cu_gabor_wavefront(to_dev(holo, cuda))
@@ -41,8 +41,10 @@ def test_xyprojection_golden(ph, cuda, golden):
     assert np.mean(to_np(arg) == g["rec_argmin"]) >= ARGMIN_AGREE
 
 
+# (6, 4096), (3, 8192), (24, 6144): pass A rows in clusters of 2 / 4 / 2 CTAs, the last
+# cluster padded with CTAs that hold no valid row
 @pytest.mark.parametrize("nx,ny", [(32, 16), (16, 64), (256, 128), (3, 6), (12, 24), (96, 48), (768, 384),
-                                   (2048, 1536), (1536, 1536)])
+                                   (2048, 1536), (1536, 1536), (6, 4096), (3, 8192), (24, 6144), (4096, 32)])
 def test_rectangular_projection(ph, cuda, nx, ny):
     holo, hf, hdz = _case(nx, seed=3, n_slow=ny)
     wf = ph.cu_gabor_wavefront(to_dev(holo, cuda))
