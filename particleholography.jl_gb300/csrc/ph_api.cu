@@ -602,7 +602,7 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
                        cudaStream_t s) {
     ReconLayout L{};
     L.batch = batch;
-    const int row_blocks_a = (nx + rows_per_cta(ny) - 1) / rows_per_cta(ny);
+    const int row_blocks_a = (nx + recon_a_rows(ny) - 1) / recon_a_rows(ny);
     for (int k0 = 0; k0 < slices; k0 += L.batch) {
         const int nb = std::min(L.batch, slices - k0);
         const int group = recon_group(nb, row_blocks_a);

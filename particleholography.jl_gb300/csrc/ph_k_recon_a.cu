@@ -3,6 +3,15 @@
 
 namespace ph {
 
+int recon_a_rows(int n) {
+    switch (n) {
+#define PH_ROWS_A(N) case N: return Shape<N, ReconA::EPT, ReconA::TT>::ROWS;
+        PH_FOR_EACH_N(PH_ROWS_A)
+#undef PH_ROWS_A
+    }
+    return 1;
+}
+
 cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s) {
     return launch_len<true>(n, b, b.nx, (nbatch + b.group - 1) / b.group, s);
 }

@@ -220,6 +220,9 @@ struct SpectrumCols : PassBase {
 // range for all 4 rows, reading its peers' rows through distributed shared
 // memory.  (Stores of 2 consecutive kx, 16 bytes, ran 3x slower.)
 struct ReconA : PassBase {
+    // 4 rows of 128 threads at N = 2048: one CTA per SM.  (One row per CTA in
+    // clusters of 4, or two in clusters of 2, measured 65 % / 59 % slower.)
+    static constexpr int TT = 512;
     template <int N>
     static constexpr int cluster() {
         return Shape<N, EPT, TT>::ROWS >= 4 ? 1 : 4 / Shape<N, EPT, TT>::ROWS;
