@@ -75,46 +75,137 @@ __device__ __forceinline__ void ccl_hook(uint32_t *lab, uint32_t a, uint32_t b, 
     }
 }
 
-// Initial parents: the smallest equal-valued earlier neighbour (NW < N < NE < W
-// in linear order), else the pixel itself.
-template <class T>
-__global__ void k_ccl_init(const T *__restrict__ img, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows) {
-    const int64_t y = (int64_t)blockIdx.x * kCclBlockY + threadIdx.y;
-    const int64_t x = (int64_t)blockIdx.y * kCclBlockX + threadIdx.x;
-    if (x >= cols || y >= rows) return;
-    const int64_t i = y * cols + x;
-    const T v = img[i];
-    int64_t p = i;
-    if (ccl_fg<T>(v)) {
-        if (x > 0 && ccl_eq(img[i - 1], v)) p = i - 1;
-        if (y % slice_rows != 0) {
-            const int64_t u = i - cols;
-            if (x + 1 < cols && ccl_eq(img[u + 1], v)) p = u + 1;
-            if (ccl_eq(img[u], v)) p = u;
-            if (x > 0 && ccl_eq(img[u - 1], v)) p = u - 1;
-        }
+// ---- tile-local phase: one CTA labels a 32 x 32 tile in shared memory
+
+constexpr int kTile = 32;
+
+// Local root of tile pixel x (parents in shared memory), shortening the path.
+__device__ __forceinline__ int ccl_lfind(volatile int *p, int x, int64_t limit, int *err) {
+    int cur = p[x];
+    if (cur == x) return x;
+    int prev = x, next;
+    int64_t it = 0;
+    while (cur > (next = p[cur])) {
+        p[prev] = next;
+        prev = cur;
+        cur = next;
+        if (++it > limit) { atomicExch(err, 1); break; }
     }
-    lab[i] = (uint32_t)p;
+    return cur;
 }
 
-// One thread per pixel: union with the equal-valued W, NW, N and NE
-// neighbours.  A batch of images is `rows / slice_rows` images stacked along
-// the rows; no union crosses an image boundary.
+__device__ __forceinline__ int ccl_lroot(volatile int *p, int x, int64_t limit, int *err) {
+    int cur = p[x], next;
+    int64_t it = 0;
+    while (cur > (next = p[cur])) {
+        cur = next;
+        if (++it > limit) { atomicExch(err, 1); break; }
+    }
+    return cur;
+}
+
+__device__ __forceinline__ void ccl_lhook(int *p, int a, int b, int64_t limit, int *err) {
+    int ra = ccl_lfind(p, a, limit, err), rb = ccl_lfind(p, b, limit, err);
+    int64_t it = 0;
+    while (ra != rb) {
+        if (ra < rb) { const int t = ra; ra = rb; rb = t; }
+        const int ret = atomicCAS(p + ra, ra, rb);
+        if (ret == ra) return;
+        ra = ret;
+        if (++it > limit) { atomicExch(err, 1); return; }
+    }
+}
+
+// Labels each 32 x 32 tile on its own: parents start at the smallest
+// equal-valued earlier neighbour inside the tile, the tile's W/NW/N/NE pairs
+// are hooked in shared memory, and every pixel leaves the global index of its
+// tile-local root.  Inside a tile, row-major tile order is global linear
+// order, so a local root is the minimum global index of its local component
+// and the global parents keep L[i] <= i.  Grid: (row tiles, column tiles),
+// block (32, 8), 4 rows per thread.
 template <class T>
-__global__ void k_ccl_union(const T *__restrict__ img, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows,
-                            int64_t limit, int *err) {
-    const int64_t y = (int64_t)blockIdx.x * kCclBlockY + threadIdx.y;
-    const int64_t x = (int64_t)blockIdx.y * kCclBlockX + threadIdx.x;
-    if (x >= cols || y >= rows) return;
+__global__ void __launch_bounds__(kCclBlockX * kCclBlockY)
+    k_ccl_local(const T *__restrict__ img, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows,
+                int64_t limit, int *err) {
+    __shared__ T sv[kTile][kTile];
+    __shared__ int sp[kTile * kTile];
+    const int64_t ty0 = (int64_t)blockIdx.x * kTile, tx0 = (int64_t)blockIdx.y * kTile;
+    const int lx = threadIdx.x;
+    constexpr int K = kTile / kCclBlockY;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int ly = threadIdx.y + k * kCclBlockY;
+        const int64_t y = ty0 + ly, x = tx0 + lx;
+        sv[ly][lx] = (y < rows && x < cols) ? img[y * cols + x] : T(0);   // outside: background
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int ly = threadIdx.y + k * kCclBlockY;
+        const int l = ly * kTile + lx;
+        const T v = sv[ly][lx];
+        int p = l;
+        if (ccl_fg<T>(v)) {
+            if (lx > 0 && ccl_eq(sv[ly][lx - 1], v)) p = l - 1;
+            if (ly > 0 && (ty0 + ly) % slice_rows != 0) {
+                if (lx + 1 < kTile && ccl_eq(sv[ly - 1][lx + 1], v)) p = l - kTile + 1;
+                if (ccl_eq(sv[ly - 1][lx], v)) p = l - kTile;
+                if (lx > 0 && ccl_eq(sv[ly - 1][lx - 1], v)) p = l - kTile - 1;
+            }
+        }
+        sp[l] = p;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int ly = threadIdx.y + k * kCclBlockY;
+        const int l = ly * kTile + lx;
+        const T v = sv[ly][lx];
+        if (!ccl_fg<T>(v)) continue;
+        if (lx > 0 && ccl_eq(sv[ly][lx - 1], v)) ccl_lhook(sp, l, l - 1, limit, err);
+        if (ly > 0 && (ty0 + ly) % slice_rows != 0) {
+            if (lx > 0 && ccl_eq(sv[ly - 1][lx - 1], v)) ccl_lhook(sp, l, l - kTile - 1, limit, err);
+            if (ccl_eq(sv[ly - 1][lx], v)) ccl_lhook(sp, l, l - kTile, limit, err);
+            if (lx + 1 < kTile && ccl_eq(sv[ly - 1][lx + 1], v)) ccl_lhook(sp, l, l - kTile + 1, limit, err);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int ly = threadIdx.y + k * kCclBlockY;
+        const int64_t y = ty0 + ly, x = tx0 + lx;
+        if (y >= rows || x >= cols) continue;
+        const int l = ly * kTile + lx;
+        const int r = ccl_fg<T>(sv[ly][lx]) ? ccl_lroot(sp, l, limit, err) : l;
+        lab[y * cols + x] = (uint32_t)((ty0 + r / kTile) * cols + tx0 + r % kTile);
+    }
+}
+
+// ---- merge across tile borders: the pairs whose earlier neighbour lies in
+// another tile (W, NW of the left column; NW, N, NE of the top row; NE of the
+// right column) are hooked in the global parents.  Grid: (row tiles, column
+// tiles), 128 threads, 94 border pixels per tile.
+template <class T>
+__global__ void k_ccl_border(const T *__restrict__ img, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows,
+                             int64_t limit, int *err) {
+    const int t = threadIdx.x;
+    int ly, lx;
+    if (t < kTile) { ly = 0; lx = t; }
+    else if (t < 2 * kTile - 1) { ly = t - (kTile - 1); lx = 0; }
+    else if (t < 3 * kTile - 2) { ly = t - (2 * kTile - 2); lx = kTile - 1; }
+    else return;
+    const int64_t y = (int64_t)blockIdx.x * kTile + ly, x = (int64_t)blockIdx.y * kTile + lx;
+    if (y >= rows || x >= cols) return;
     const int64_t i = y * cols + x;
     const T v = img[i];
     if (!ccl_fg<T>(v)) return;
-    if (x > 0 && ccl_eq(img[i - 1], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)(i - 1), limit, err);
+    if (lx == 0 && x > 0 && ccl_eq(img[i - 1], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)(i - 1), limit, err);
     if (y % slice_rows != 0) {
         const int64_t u = i - cols;
-        if (x > 0 && ccl_eq(img[u - 1], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)(u - 1), limit, err);
-        if (ccl_eq(img[u], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)u, limit, err);
-        if (x + 1 < cols && ccl_eq(img[u + 1], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)(u + 1), limit, err);
+        if ((lx == 0 || ly == 0) && x > 0 && ccl_eq(img[u - 1], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)(u - 1), limit, err);
+        if (ly == 0 && ccl_eq(img[u], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)u, limit, err);
+        if ((ly == 0 || lx == kTile - 1) && x + 1 < cols && ccl_eq(img[u + 1], v))
+            ccl_hook(lab, (uint32_t)i, (uint32_t)(u + 1), limit, err);
     }
 }
 
@@ -141,9 +232,9 @@ static cudaError_t ccl_run(const T *img, uint32_t *lab, int64_t rows, int64_t co
     const int tpb = 256;
     const unsigned g1 = (unsigned)((n + tpb - 1) / tpb);
     dim3 b2(kCclBlockX, kCclBlockY);
-    dim3 g2((unsigned)((rows + kCclBlockY - 1) / kCclBlockY), (unsigned)((cols + kCclBlockX - 1) / kCclBlockX));
-    k_ccl_init<T><<<g2, b2, 0, s>>>(img, lab, rows, cols, slice_rows);
-    k_ccl_union<T><<<g2, b2, 0, s>>>(img, lab, rows, cols, slice_rows, limit, err);
+    dim3 gt((unsigned)((rows + kTile - 1) / kTile), (unsigned)((cols + kTile - 1) / kTile));
+    k_ccl_local<T><<<gt, b2, 0, s>>>(img, lab, rows, cols, slice_rows, limit, err);
+    k_ccl_border<T><<<gt, 128, 0, s>>>(img, lab, rows, cols, slice_rows, limit, err);
     k_ccl_compress<T><<<g1, tpb, 0, s>>>(img, lab, n, limit, err);
     k_ccl_background<T><<<g1, tpb, 0, s>>>(img, lab, n, slice_rows * cols);
     *launches += 4;
