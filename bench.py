@@ -55,7 +55,23 @@ CONFIGS = {
                zmax=100000.0, gs_iters=2, gs_sep=5000.0, threshold=0.1, seed=2,
                workload="gs2048_pr2_recon64_profile"),
 }
+# Mixed batch: (n_fast, n_slow, count) size classes; per item slices ~ U{32..512} and
+# dz ~ U(0.1, 0.5) mm drawn from numpy PCG64(1000 + i); reconstructed from z0 = 5 mm.
+C4_CLASSES = [(512, 512, 32), (1024, 1024, 32), (2048, 1536, 16), (2048, 2048, 16)]
+CONFIGS["c4"] = dict(n=2048, slices=0, dz=0.0, z0=5000.0, discs=200, dmin=10.0, dmax=60.0, zmin=5000.0,
+                     zmax=100000.0, gs_iters=0, gs_sep=0.0, threshold=0.1, seed=4, kind="batch",
+                     workload="batch96_mixed_512_1024_1536x2048_2048_proj_argmin")
 L2_FLUSH_BYTES = 512 << 20
+
+
+def c4_items():
+    """(n_fast, n_slow, slices, dz_um) of the 96 items of the mixed batch."""
+    out = []
+    for nx, ny, count in C4_CLASSES:
+        for _ in range(count):
+            rng = np.random.default_rng(1000 + len(out))
+            out.append((nx, ny, int(rng.integers(32, 513)), float(rng.uniform(100.0, 500.0))))
+    return out
 
 
 def _peaks():
@@ -275,6 +291,8 @@ def main():
 
     if args.impl == "reference":
         return reference_arm(args, cfg, rank, world)
+    if cfg.get("kind") == "batch":
+        return batch_main(args, cfg, rank, world, local)
 
     import torch
     import torch.distributed as dist
@@ -486,6 +504,153 @@ def _traffic_from_profiles(kernel: str, config: str):
                 except ValueError:
                     pass
     return None
+
+
+def batch_main(args, cfg, rank, world, local):
+    """The mixed batch (C4) through ph_batch_plan / ph_batch_run: 96 holograms of
+    four sizes, each with its own slice count and dz, as one graph launch per step."""
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+    import __graft_entry__ as g
+    ph = g.load_package()
+    from ph_gb300 import _lib, synth
+    ctx = _lib.default_context(local)
+    items_spec = c4_items()
+    holos, sqr, host = {}, {}, {}
+    for ci, (nx, ny, _) in enumerate(C4_CLASSES):
+        spec = synth.HologramSpec(seed=cfg["seed"] + 100 * ci + 1000 * rank, n=nx, n_slow=ny, count=cfg["discs"],
+                                  dmin=cfg["dmin"], dmax=cfg["dmax"], zmin=cfg["zmin"], zmax=cfg["zmax"],
+                                  wavlen=LAM, dx=DX)
+        holos[(nx, ny)] = synth.synth_hologram(spec, local)
+        host[(nx, ny)] = torch.empty((ny, nx), dtype=torch.float32, pin_memory=True)
+        host[(nx, ny)].copy_(holos[(nx, ny)])
+        sqr[(nx, ny)] = ph.cu_transfer_sqrt_arr(nx, LAM, DX, device=local, n_slow=ny)
+    items = []
+    for nx, ny, S, dz in items_spec:
+        hf, hdz = ph.cu_transfer(-cfg["z0"], nx, LAM, sqr[(nx, ny)]), ph.cu_transfer(-dz, nx, LAM, sqr[(nx, ny)])
+        items.append({"hologram": holos[(nx, ny)], "transfer_front": hf, "transfer_dz": hdz, "slices": S})
+    voxels = sum(nx * ny * S for nx, ny, S, _ in items_spec)
+    batch = ph.ReconBatch(items, lanes=4)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        batch.run()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = ctx.launches
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        batch.run()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches - l0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t = torch.tensor([sum(step_ms)], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    value = voxels * args.steps * world / (total_ms / 1e3) / 1e6
+
+    e2e = None
+    if not args.no_e2e:
+        outs_host = [torch.empty(p.shape, dtype=torch.float32, pin_memory=True) for p in batch.proj]
+
+        def e2e_step():
+            for k in holos:
+                holos[k].copy_(host[k], non_blocking=True)
+            proj, _ = batch.run()
+            for o, p in zip(outs_host, proj):
+                o.copy_(p, non_blocking=True)
+            torch.cuda.synchronize()
+
+        e2e_step()
+        e_ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2e_step()
+            e_ms.append((time.perf_counter() - t0) * 1e3)
+        e2e = {"value": round(voxels * args.steps / (sum(e_ms) / 1e3) / 1e6, 2), "unit": "Mvoxel/s",
+               "h2d_bytes_per_step": int(sum(h.numel() * 4 for h in host.values())),
+               "d2h_bytes_per_step": int(sum(o.numel() * 4 for o in outs_host)),
+               "p50_batch_ms": round(statistics.median(e_ms), 3), "p99_batch_ms": round(float(np.percentile(e_ms, 99)), 3)}
+
+    standin = None
+    if not args.no_standin:
+        fft2, ifft2, fsh, ifsh = torch.fft.fft2, torch.fft.ifft2, torch.fft.fftshift, torch.fft.ifftshift
+
+        def standin_step():
+            for it in items:
+                h = it["hologram"]
+                x = fsh(fft2(torch.complex(torch.sqrt(h), torch.zeros_like(h)))) * it["transfer_front"].data
+                proj = torch.full(h.shape, float("inf"), device=dev)
+                for k in range(it["slices"]):
+                    if k > 0:
+                        x = x * it["transfer_dz"].data
+                    img = ifft2(ifsh(x))
+                    proj = torch.minimum(proj, torch.abs(img * torch.conj(img)).float())
+        standin_step()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        standin_step()
+        b.record()
+        torch.cuda.synchronize()
+        sms = a.elapsed_time(b)
+        standin = {"value": round(voxels / (sms / 1e3) / 1e6, 2), "unit": "Mvoxel/s", "ms_per_step": round(sms, 3),
+                   "what": "cuFFT stand-in of the reference's kernel sequence, one item after another (host loop)"}
+
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        from oracle import ref_semantics as ref
+        secs = 0.0
+        for (nx, ny, _) in C4_CLASSES:
+            hn = holos[(nx, ny)].cpu().numpy()
+            d = ref.transfer_sqrt_arr(nx, LAM, DX, n_slow=ny)
+            hf, hdz = ref.transfer(-cfg["z0"], nx, LAM, d), ref.transfer(-200.0, nx, LAM, d)
+            t0 = time.perf_counter()
+            ref.reconst_xyprojection(ref.gabor_wavefront(hn), hf, hdz, 2)
+            per_slice = (time.perf_counter() - t0) / 2
+            secs += per_slice * sum(S for x, y, S, _ in items_spec if (x, y) == (nx, ny))
+        cpu = {"value": round(voxels / secs / 1e6, 3), "unit": "Mvoxel/s", "cores": len(os.sched_getaffinity(0)),
+               "kind": "port", "sample": "oracle FP32 (numpy/scipy.fft workers=all): 2 slices per size class, "
+                                         "scaled by each class's total slices"}
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    line = {
+        "metric": "reconstructed Mvoxel/s + p99 frame latency, chosen vs plain FP32 form, 1 GB300",
+        "value": round(value, 2), "unit": "Mvoxel/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (one seeded disc hologram per size class, shared by the class's items)",
+        "config": {"workload": cfg["workload"], "items": len(items_spec), "voxels_per_step": voxels,
+                   "lanes": 4, "form": "fp32-stockham", "l2": "flushed (512 MiB write) before every timed step",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "p50_frame_ms": round(statistics.median(step_ms), 3),
+        "p99_frame_ms": round(float(np.percentile(step_ms, 99)), 3),
+        "gpu_launches": int(launches), "roofline": None, "cpu_baseline": cpu, "e2e": e2e,
+        "cufft_standin": standin, "clocks": clk,
+        "batch_scratch_bytes": batch.scratch_bytes,
+    }
+    print(json.dumps(line))
+    batch.close()
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
 
 
 def reference_arm(args, cfg, rank, world):

@@ -190,6 +190,43 @@ PH_API int32_t ph_reconst_vol_padded(ph_ctx *ctx, uint8_t *vol, float *proj, con
                               int32_t n_fast, int32_t n_slow, int32_t slices,
                               int32_t return_dtype, void *stream);
 
+/* ---- batches of reconstructions ------------------------------------------------- */
+
+/* No single reference counterpart: a batch of cu_get_reconst_xyprojection calls
+ * (holofunc.jl:248-266), one per hologram, each with its own size, transfer
+ * functions and slice count (the reference runs them one after another from
+ * its host loop).  One item: */
+typedef struct ph_recon_item {
+    const float *hologram;   /* Float32 [n_slow][n_fast]: wavefront = sqrt(hologram) + 0i
+                                (cu_gabor_wavefront, holofunc.jl:80-82); or NULL */
+    const void *wavefront;   /* ComplexF32 [n_slow][n_fast], used when hologram is NULL */
+    const void *tf_front;    /* ComplexF32 centred transfer to the first slice */
+    const void *tf_dz;       /* ComplexF32 centred transfer between slices */
+    float *proj;             /* out: [n_slow][n_fast] minimum over slices of |u|^2 */
+    int32_t *argmin;         /* out (nullable): first slice attaining it */
+    int32_t n_fast, n_slow, slices;
+} ph_recon_item;
+
+typedef struct ph_batch ph_batch;
+
+/* Plans a batch of cu_get_reconst_xyprojection calls (holofunc.jl:248-266):
+ * validates every item (the same checks and messages as
+ * ph_reconst_xyproj), spreads the items over `lanes` concurrent streams (1-16;
+ * longest first, each to the least loaded lane), allocates the lanes' scratch
+ * (its own, outside the context's arena) and records the whole batch as one
+ * CUDA graph.  The plan keeps the item pointers: the buffers must stay valid
+ * until ph_batch_destroy.  Synchronises the context's work. */
+PH_API int32_t ph_batch_plan(ph_ctx *ctx, const ph_recon_item *items, int32_t count, int32_t lanes,
+                             ph_batch **out);
+/* Runs a planned batch on `stream` (one graph launch); the items' outputs are
+ * written as by one cu_get_reconst_xyprojection (holofunc.jl:248-266) /
+ * ph_reconst_xyproj call each, with identical results.  Asynchronous. */
+PH_API int32_t ph_batch_run(ph_batch *batch, void *stream);
+/* Bytes of device scratch the plan holds (no reference counterpart). */
+PH_API size_t ph_batch_scratch_bytes(const ph_batch *batch);
+/* Frees the plan (waits for its launches to finish; no reference counterpart). */
+PH_API void ph_batch_destroy(ph_batch *batch);
+
 /* ---- synthetic input ----------------------------------------------------------- */
 
 /* No reference counterpart (the reference ships no generator): the seeded

@@ -9,6 +9,7 @@ The directory name is not a Python identifier; load the package with
 ``__graft_entry__.load_package()`` (it registers it as ``ph_gb300``).
 """
 from . import _lib
+from .batch import ReconBatch
 from .ccl import (count_labels, cu_bounding_rectangles, cu_connected_component_labeling,
                   cu_connected_component_labeling_batch, cu_find_valid_labels)
 from .frequency_filters import (cu_apply_low_pass_filter, cu_apply_low_pass_filter_, cu_rectangle_filter,

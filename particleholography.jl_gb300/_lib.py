@@ -71,7 +71,17 @@ SIGNATURES = {
     "ph_ccl_count_noalloc": (_i32, [_vp, _vp, _i64, _vp]),
     "ph_noalloc_last_error": (ctypes.c_char_p, []),
     "ph_ccl_boxes": (_i32, [_vp, _vp, _i64, ctypes.POINTER(_i64), _vp, _i64, _i64, _i64, _vp]),
+    "ph_batch_plan": (_i32, [_vp, _vp, _i32, _i32, ctypes.POINTER(_vp)]),
+    "ph_batch_run": (_i32, [_vp, _vp]),
+    "ph_batch_scratch_bytes": (_sz, [_vp]),
+    "ph_batch_destroy": (None, [_vp]),
 }
+
+
+class ReconItem(ctypes.Structure):
+    """ph_recon_item (phgb300.h)."""
+    _fields_ = [("hologram", _vp), ("wavefront", _vp), ("tf_front", _vp), ("tf_dz", _vp), ("proj", _vp),
+                ("argmin", _vp), ("n_fast", _i32), ("n_slow", _i32), ("slices", _i32)]
 
 _lib = None
 _lock = threading.Lock()            # guards loading the library

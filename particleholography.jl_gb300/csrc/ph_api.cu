@@ -19,6 +19,19 @@
 #include "ph_ctx.h"
 #include "ph_launch.cuh"
 
+// A planned batch of reconstructions: its items, lanes, own scratch and the
+// recorded graph.
+struct ph_batch {
+    ph_ctx *ctx = nullptr;
+    std::vector<ph_recon_item> items;
+    std::vector<int> lane_of;
+    int lanes = 1;
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    cudaGraphExec_t exec = nullptr;
+    int64_t kernels = 0;
+};
+
 namespace ph {
 cudaError_t ccl_launch(const void *img, bool is_bool, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows,
                        int64_t limit, int *err, cudaStream_t s, int64_t *launches);
@@ -474,11 +487,19 @@ struct Spectrum {
 };
 
 // Forward FFT of the (optionally mean-padded) wavefront and the spectrum state.
-// nx, ny: transform size; a1: scratch [nx][ny] complex.
+// nx, ny: transform size; a1: scratch [nx][ny] complex.  With `holo` (and wf
+// NULL) the wavefront is sqrt(holo) + 0i, formed in the first FFT stage.
 int issue_spectrum(ph_ctx *ctx, const float2 *wf, const float2 *hf, const float2 *hdz, int nx, int ny,
                    bool padded, int nin_x, int nin_y, float2 *a1, float4 *state, const float2 *tw_x,
-                   const float2 *tw_y, double *acc, float2 *mean, cudaStream_t s) {
-    if (padded) {
+                   const float2 *tw_y, double *acc, float2 *mean, cudaStream_t s, const float *holo = nullptr) {
+    if (holo != nullptr) {
+        FwdRowsT<FWD_SQRT_REAL> f{};
+        f.src_real = holo;
+        f.dst = a1;
+        f.tw = tw_x;
+        f.nrows = ny;
+        PH_TRY(pass(ctx, s, "fwd_rows", [&] { return launch_fwd_rows(nx, f, s); }));
+    } else if (padded) {
         PH_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(double), s), "cudaMemsetAsync");
         k_sum_c64<<<256, 256, 0, s>>>(wf, (size_t)nin_x * nin_y, acc);
         k_mean_finish<<<1, 1, 0, s>>>(acc, (double)nin_x * nin_y, mean);
@@ -674,6 +695,23 @@ int issue_propagate(ph_ctx *ctx, float2 *out, const float2 *in, const float2 *h,
     r.nrows = ny;
     PH_TRY(pass(ctx, s, "inv_rows",[&] { return launch_gs_row(nx, r, s); }));
     return PH_OK;
+}
+
+// ---------------------------------------------------------------- batches
+
+// Longest-processing-time assignment of items (work = pixels x slices) to lanes.
+std::vector<int> assign_lanes(const ph_recon_item *items, int count, int lanes) {
+    std::vector<int> order(count), lane(count, 0);
+    for (int i = 0; i < count; ++i) order[i] = i;
+    auto work = [&](int i) { return (double)items[i].n_fast * items[i].n_slow * items[i].slices; };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work(a) > work(b); });
+    std::vector<double> load(lanes, 0.0);
+    for (int i : order) {
+        const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        lane[i] = l;
+        load[l] += work(i);
+    }
+    return lane;
 }
 
 }  // namespace
@@ -1113,6 +1151,157 @@ int32_t ph_reconst_xyproj(ph_ctx *ctx, float *proj, int32_t *argmin, const void 
                        static_cast<const float2 *>(tf_front), static_cast<const float2 *>(tf_dz), n_fast, n_slow,
                        slices, s));
     PH_LEAVE(ctx);
+}
+
+int32_t ph_batch_plan(ph_ctx *ctx, const ph_recon_item *items, int32_t count, int32_t lanes, ph_batch **out) {
+    PH_ENTER(ctx, nullptr);
+    PH_NONNULL(out, "out");
+    *out = nullptr;
+    if (count < 0 || (count > 0 && items == nullptr)) { set_err(ctx, "items must hold count >= 0 records"); return PH_ERR_INVALID; }
+    if (lanes < 1 || lanes > 16) { set_err(ctx, "lanes must be in 1..16. Got %d.", lanes); return PH_ERR_INVALID; }
+    for (int i = 0; i < count; ++i) {
+        const ph_recon_item &it = items[i];
+        if (it.hologram == nullptr && it.wavefront == nullptr) {
+            set_err(ctx, "item %d: hologram and wavefront are both NULL", i);
+            return PH_ERR_INVALID;
+        }
+        if (it.tf_front == nullptr || it.tf_dz == nullptr) { set_err(ctx, "item %d: transfer functions must not be NULL", i); return PH_ERR_INVALID; }
+        if (it.proj == nullptr && it.argmin == nullptr) { set_err(ctx, "item %d: proj and argmin are both NULL", i); return PH_ERR_INVALID; }
+        if (it.slices < 1) { set_err(ctx, "item %d: slices must be >= 1. Got %d.", i, it.slices); return PH_ERR_SIZE; }
+        PH_TRY(check_len(ctx, it.n_fast, it.n_slow));
+    }
+    lanes = std::max(1, std::min(lanes, std::max(count, 1)));
+    auto *b = new ph_batch();
+    b->ctx = ctx;
+    b->items.assign(items, items + count);
+    b->lane_of = assign_lanes(items, count, lanes);
+    b->lanes = lanes;
+    // per-lane scratch: the largest layout among the lane's items
+    std::vector<size_t> lane_bytes(lanes, 0), lane_off(lanes, 0);
+    for (int i = 0; i < count; ++i) {
+        const ReconLayout L = recon_layout(ctx, items[i].n_fast, items[i].n_slow, items[i].n_slow, items[i].n_fast,
+                                           items[i].slices);
+        lane_bytes[b->lane_of[i]] = std::max(lane_bytes[b->lane_of[i]], L.total);
+    }
+    size_t total = 0;
+    for (int l = 0; l < lanes; ++l) {
+        lane_off[l] = total;
+        total += (lane_bytes[l] + kAlign - 1) / kAlign * kAlign;
+    }
+    int st = PH_OK;
+    std::vector<cudaStream_t> ls(lanes, nullptr);
+    std::vector<cudaEvent_t> join(lanes, nullptr);
+    cudaEvent_t fork = nullptr;
+    auto fail = [&](int code) {
+        for (auto x : ls) if (x) cudaStreamDestroy(x);
+        for (auto e : join) if (e) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        if (b->scratch) cudaFree(b->scratch);
+        delete b;
+        cudaGetLastError();
+        return code;
+    };
+    if (ctx->budget && total + ctx->scratch_bytes > ctx->budget) {
+        set_err(ctx, "batch scratch of %zu bytes exceeds the context's HBM budget of %zu bytes", total, ctx->budget);
+        return fail(PH_ERR_OOM);
+    }
+    if (total > 0 && cudaMalloc(&b->scratch, total) != cudaSuccess) {
+        set_err(ctx, "cudaMalloc of %zu bytes of batch scratch failed", total);
+        return fail(PH_ERR_OOM);
+    }
+    b->scratch_bytes = total;
+    for (int i = 0; i < count; ++i) {   // twiddle tables exist before the capture
+        const float2 *tw = nullptr;
+        if ((st = get_twiddles(ctx, items[i].n_fast, nullptr, &tw)) != PH_OK) return fail(st);
+        if ((st = get_twiddles(ctx, items[i].n_slow, nullptr, &tw)) != PH_OK) return fail(st);
+    }
+    for (int l = 0; l < lanes; ++l) {
+        if (cudaStreamCreateWithFlags(&ls[l], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&join[l], cudaEventDisableTiming) != cudaSuccess) {
+            set_err(ctx, "could not create the batch lanes");
+            return fail(PH_ERR_CUDA);
+        }
+    }
+    if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) return fail(PH_ERR_CUDA);
+    // record: capture stream -> fork to the lanes -> each lane's items in turn -> join
+    cudaStream_t cs = ctx->capture_stream;
+    const int64_t l0 = ctx->launches.load();
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return fail(PH_ERR_CUDA);
+    cudaEventRecord(fork, cs);
+    for (int l = 0; l < lanes && st == PH_OK; ++l) {
+        cudaStreamWaitEvent(ls[l], fork, 0);
+        char *base = static_cast<char *>(b->scratch) + lane_off[l];
+        for (int i = 0; i < count && st == PH_OK; ++i) {
+            if (b->lane_of[i] != l) continue;
+            const ph_recon_item &it = items[i];
+            const int nx = it.n_fast, ny = it.n_slow;
+            const ReconLayout L = recon_layout(ctx, nx, ny, ny, nx, it.slices);
+            const float2 *tw_x = ctx->tw[nx], *tw_y = ctx->tw[ny];
+            auto *state = reinterpret_cast<float4 *>(base + L.state);
+            auto *p64 = reinterpret_cast<unsigned long long *>(base + L.p64);
+            auto *t = reinterpret_cast<float2 *>(base + L.t);
+            st = issue_spectrum(ctx, static_cast<const float2 *>(it.wavefront), static_cast<const float2 *>(it.tf_front),
+                                static_cast<const float2 *>(it.tf_dz), nx, ny, false, nx, ny,
+                                reinterpret_cast<float2 *>(base + L.a1), state, tw_x, tw_y,
+                                reinterpret_cast<double *>(base + L.acc), reinterpret_cast<float2 *>(base + L.mean),
+                                ls[l], it.hologram);
+            if (st != PH_OK) break;
+            if (cudaMemsetAsync(p64, 0xff, sizeof(unsigned long long) * nx * ny, ls[l]) != cudaSuccess) {
+                st = PH_ERR_CUDA;
+                break;
+            }
+            st = issue_recon_slices(ctx, RK_PROJ, it.proj, it.argmin, nullptr, PH_F32, nx, ny, nx, ny, 0, 0,
+                                    it.slices, L.batch, state, t, p64, tw_x, tw_y, true, ls[l]);
+        }
+        cudaEventRecord(join[l], ls[l]);
+        cudaStreamWaitEvent(cs, join[l], 0);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(cs, &g);
+    b->kernels = ctx->launches.load() - l0;
+    ctx->launches = l0;
+    if (st != PH_OK || ec != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (st == PH_OK) st = cuda_status(ctx, ec, "cudaStreamEndCapture");
+        return fail(st);
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&b->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        st = cuda_status(ctx, ei, "cudaGraphInstantiate");
+        return fail(st);
+    }
+    for (auto x : ls) cudaStreamDestroy(x);
+    for (auto e : join) cudaEventDestroy(e);
+    cudaEventDestroy(fork);
+    *out = b;
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_batch_run(ph_batch *batch, void *stream) {
+    if (batch == nullptr) return PH_ERR_INVALID;
+    ph_ctx *ctx = batch->ctx;
+    PH_ENTER(ctx, stream);
+    if (batch->exec) {
+        PH_CUDA(cudaGraphLaunch(batch->exec, s), "cudaGraphLaunch");
+        ctx->launches += batch->kernels;
+    }
+    PH_LEAVE(ctx);
+}
+
+size_t ph_batch_scratch_bytes(const ph_batch *batch) { return batch ? batch->scratch_bytes : 0; }
+
+void ph_batch_destroy(ph_batch *batch) {
+    if (batch == nullptr) return;
+    {
+        std::lock_guard<std::mutex> lk(batch->ctx->mu);
+        DeviceGuard g(batch->ctx->device);
+        cudaDeviceSynchronize();
+        if (batch->exec) cudaGraphExecDestroy(batch->exec);
+        if (batch->scratch) cudaFree(batch->scratch);
+        cudaGetLastError();
+    }
+    delete batch;
 }
 
 int32_t ph_reconst_vol(ph_ctx *ctx, void *vol, int32_t vol_dtype, float *proj, const void *wf, const void *tf_front,

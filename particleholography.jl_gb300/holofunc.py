@@ -67,33 +67,39 @@ def _return_code(return_type):
 
 # ------------------------------------------------------------------ transfer functions
 
-def cu_transfer_sqrt_arr(datlen: int, wavlen: float, dx: float, device: int | None = None) -> CuTransferSqrtPart:
-    """holofunc.jl:30-36: the Float32 square-root term of the transfer function."""
+def cu_transfer_sqrt_arr(datlen: int, wavlen: float, dx: float, device: int | None = None,
+                         n_slow: int | None = None) -> CuTransferSqrtPart:
+    """holofunc.jl:30-36: the Float32 square-root term of the transfer function.
+    ``n_slow`` (an extension; the reference is square): rows of a datlen-wide grid."""
     dev = torch.cuda.current_device() if device is None else device
-    out = torch.empty((datlen, datlen), dtype=torch.float32, device=f"cuda:{dev}")
+    ny = datlen if n_slow is None else int(n_slow)
+    out = torch.empty((ny, datlen), dtype=torch.float32, device=f"cuda:{dev}")
     ctx, s = _ctx_stream(out)
-    ctx.call("ph_transfer_sqrt", out.data_ptr(), datlen, datlen, float(wavlen), float(dx), s)
+    ctx.call("ph_transfer_sqrt", out.data_ptr(), datlen, ny, float(wavlen), float(dx), s)
     return CuTransferSqrtPart(out)
 
 
 def cu_transfer(z0: float, datLen: int, wavLen: float, d_sqr: CuTransferSqrtPart) -> CuTransfer:
     """holofunc.jl:61-67: ``exp(2im*pi*z0/wavLen*sqrt(d_sqr))`` as ComplexF32."""
     d = _need(_data(d_sqr), torch.float32, "d_sqr")
-    if tuple(d.shape) != (datLen, datLen):
+    if d.dim() != 2 or int(d.shape[1]) != datLen:   # rows may differ (non-square grids from n_slow)
         raise AssertionError(f"d_sqr must have size ({datLen}, {datLen}). Got {_jsize(d)}.")
-    out = torch.empty((datLen, datLen), dtype=torch.complex64, device=d.device)
+    ny = int(d.shape[0])
+    out = torch.empty((ny, datLen), dtype=torch.complex64, device=d.device)
     ctx, s = _ctx_stream(out)
-    ctx.call("ph_transfer", out.data_ptr(), d.data_ptr(), datLen, datLen, float(z0), float(wavLen), s)
+    ctx.call("ph_transfer", out.data_ptr(), d.data_ptr(), datLen, ny, float(z0), float(wavLen), s)
     return CuTransfer(out)
 
 
-def cu_transfer_fp64(z: float, datlen: int, wavlen: float, dx: float, device: int | None = None) -> CuTransfer:
+def cu_transfer_fp64(z: float, datlen: int, wavlen: float, dx: float, device: int | None = None,
+                     n_slow: int | None = None) -> CuTransfer:
     """No reference counterpart: the transfer function with the square-root term
     in FP64 (exact physics) on the same centred grid as ``cu_transfer``."""
     dev = torch.cuda.current_device() if device is None else device
-    out = torch.empty((datlen, datlen), dtype=torch.complex64, device=f"cuda:{dev}")
+    ny = datlen if n_slow is None else int(n_slow)
+    out = torch.empty((ny, datlen), dtype=torch.complex64, device=f"cuda:{dev}")
     ctx, s = _ctx_stream(out)
-    ctx.call("ph_transfer_fp64", out.data_ptr(), datlen, datlen, float(z), float(wavlen), float(dx), s)
+    ctx.call("ph_transfer_fp64", out.data_ptr(), datlen, ny, float(z), float(wavlen), float(dx), s)
     return CuTransfer(out)
 
 

@@ -32,6 +32,11 @@ class HologramSpec:
     dx: float = 10.0
     sigma: float = 0.01
     z_sensor: float = 0.0
+    n_slow: int | None = None   # rows (slow axis); None = n (square)
+
+    @property
+    def ny(self) -> int:
+        return self.n if self.n_slow is None else self.n_slow
 
 
 def draw_discs(spec: HologramSpec) -> np.ndarray:
@@ -39,7 +44,7 @@ def draw_discs(spec: HologramSpec) -> np.ndarray:
     rng = np.random.Generator(np.random.PCG64(spec.seed))
     d = rng.uniform(spec.dmin, spec.dmax, spec.count)
     x = rng.uniform(0.0, spec.n * spec.dx, spec.count)
-    y = rng.uniform(0.0, spec.n * spec.dx, spec.count)
+    y = rng.uniform(0.0, spec.ny * spec.dx, spec.count)
     z = rng.uniform(spec.zmin, spec.zmax, spec.count)
     return np.ascontiguousarray(np.stack([x, y, d, z], axis=1), dtype=np.float64)
 
@@ -47,19 +52,19 @@ def draw_discs(spec: HologramSpec) -> np.ndarray:
 def draw_noise(spec: HologramSpec, stream: int = 1) -> np.ndarray:
     """Sensor noise of the hologram: N(0, sigma^2) from the stream ``seed + stream``."""
     rng = np.random.Generator(np.random.PCG64(spec.seed + stream))
-    return rng.normal(0.0, spec.sigma, (spec.n, spec.n)).astype(np.float32)
+    return rng.normal(0.0, spec.sigma, (spec.ny, spec.n)).astype(np.float32)
 
 
 def synth_hologram(spec: HologramSpec, device: int | None = None, noise: bool = True,
                    noise_stream: int = 1) -> torch.Tensor:
-    """A Float32 CUDA tensor of shape (n, n): the seeded hologram (noisy
+    """A Float32 CUDA tensor of shape (ny, n): the seeded hologram (noisy
     intensities clamped at 0, as a sensor records them)."""
     dev = torch.cuda.current_device() if device is None else device
-    out = torch.empty((spec.n, spec.n), dtype=torch.float32, device=f"cuda:{dev}")
+    out = torch.empty((spec.ny, spec.n), dtype=torch.float32, device=f"cuda:{dev}")
     discs = draw_discs(spec)
     nz = torch.from_numpy(draw_noise(spec, noise_stream)).to(out.device) if noise and spec.sigma > 0 else None
     ctx = _lib.default_context(dev)
-    ctx.call("ph_synth_hologram", out.data_ptr(), spec.n, spec.n, discs.ctypes.data, int(spec.count),
+    ctx.call("ph_synth_hologram", out.data_ptr(), spec.n, spec.ny, discs.ctypes.data, int(spec.count),
              float(spec.wavlen), float(spec.dx), float(spec.z_sensor), nz.data_ptr() if nz is not None else None,
              torch.cuda.current_stream(dev).cuda_stream)
     if nz is not None:

@@ -1,0 +1,81 @@
+"""Batches of projections (ph_batch_plan / ph_batch_run): every item equals its
+own single cu_get_reconst_xyprojection call bit for bit, the plan replays with
+new input contents, and bad items are rejected before anything runs."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import ref_semantics as ref
+from phtest import REL_L2, rel_l2, to_dev, to_np
+
+pytestmark = pytest.mark.gpu
+
+LAM, DX = 0.6328, 10.0
+
+
+def _item(cuda, nx, ny, slices, seed, as_hologram, z0=-1500.0, dz=-150.0):
+    rng = np.random.default_rng(seed)
+    holo = rng.uniform(0.1, 1.0, (ny, nx)).astype(np.float32)
+    d = ref.transfer_sqrt_arr(nx, LAM, DX, n_slow=ny)
+    hf, hdz = ref.transfer(z0, nx, LAM, d), ref.transfer(dz - seed, nx, LAM, d)
+    it = {"transfer_front": to_dev(hf, cuda), "transfer_dz": to_dev(hdz, cuda), "slices": slices}
+    if as_hologram:
+        it["hologram"] = to_dev(holo, cuda)
+    else:
+        it["wavefront"] = to_dev(ref.gabor_wavefront(holo), cuda)
+    return it, holo, hf, hdz
+
+
+def _single(ph, it):
+    wf = it["wavefront"] if "wavefront" in it else ph.cu_gabor_wavefront(it["hologram"]).data
+    return ph.cu_get_reconst_xyprojection(ph.CuWavefront(wf), ph.CuTransfer(it["transfer_front"]),
+                                          ph.CuTransfer(it["transfer_dz"]), it["slices"], return_argmin=True)
+
+
+SHAPES = [(64, 64, 5), (128, 256, 9), (96, 48, 3), (512, 512, 17), (3, 6, 2), (256, 128, 33), (1024, 1024, 4),
+          (32, 32, 1)]
+
+
+@pytest.mark.parametrize("lanes", [1, 3, 8])
+def test_batch_equals_single_calls(ph, cuda, lanes):
+    items = [_item(cuda, nx, ny, s, seed=i, as_hologram=(i % 2 == 0))[0] for i, (nx, ny, s) in enumerate(SHAPES)]
+    batch = ph.ReconBatch(items, lanes=lanes)
+    proj, arg = batch.run()
+    torch.cuda.synchronize()
+    assert batch.scratch_bytes > 0
+    for it, p, a in zip(items, proj, arg):
+        p1, a1 = _single(ph, it)
+        assert torch.equal(p, p1)
+        assert torch.equal(a, a1)
+    batch.close()
+
+
+def test_batch_against_oracle_and_replay(ph, cuda):
+    it0, holo0, hf0, hdz0 = _item(cuda, 256, 256, 12, seed=5, as_hologram=True)
+    it1, holo1, hf1, hdz1 = _item(cuda, 128, 64, 7, seed=6, as_hologram=False)
+    batch = ph.ReconBatch([it0, it1], lanes=2)
+    proj, _ = batch.run()
+    want0 = ref.reconst_xyprojection(ref.gabor_wavefront(holo0), hf0, hdz0, 12)
+    want1 = ref.reconst_xyprojection(ref.gabor_wavefront(holo1), hf1, hdz1, 7)
+    assert rel_l2(to_np(proj[0]), want0) < REL_L2
+    assert rel_l2(to_np(proj[1]), want1) < REL_L2
+    # replay with new hologram contents in the same buffer
+    new = np.random.default_rng(99).uniform(0.1, 1.0, holo0.shape).astype(np.float32)
+    it0["hologram"].copy_(torch.from_numpy(new))
+    proj, _ = batch.run()
+    want0 = ref.reconst_xyprojection(ref.gabor_wavefront(new), hf0, hdz0, 12)
+    assert rel_l2(to_np(proj[0]), want0) < REL_L2
+    batch.close()
+
+
+def test_batch_rejects_bad_items(ph, cuda):
+    good = _item(cuda, 64, 64, 3, seed=1, as_hologram=True)[0]
+    bad = dict(good, slices=0)
+    with pytest.raises(AssertionError):
+        ph.ReconBatch([good, bad])
+    odd = _item(cuda, 10, 10, 3, seed=2, as_hologram=True)[0]
+    with pytest.raises(ph._lib.PhError):   # length 10 is not 2^a or 3 * 2^a
+        ph.ReconBatch([good, odd])
+    mismatched = dict(good, transfer_dz=torch.zeros((32, 64), dtype=torch.complex64, device=good["hologram"].device))
+    with pytest.raises(AssertionError):
+        ph.ReconBatch([mismatched])
