@@ -227,6 +227,46 @@ PH_API size_t ph_batch_scratch_bytes(const ph_batch *batch);
 /* Frees the plan (waits for its launches to finish; no reference counterpart). */
 PH_API void ph_batch_destroy(ph_batch *batch);
 
+/* ---- serving --------------------------------------------------------------------- */
+
+/* A request queue in front of cu_get_reconst_xyprojection (holofunc.jl:248-266)
+ * for a stream of holograms.  The server owns `lanes` CUDA streams, each with
+ * scratch for the largest request it accepts; a request goes to the lane with
+ * the fewest requests in flight and runs there asynchronously.  The transfer
+ * functions are built as the reference builds them (cu_transfer_sqrt_arr +
+ * cu_transfer, holofunc.jl:30-67) for Hf = H(-z0) and Hdz = H(-dz) and kept in
+ * an LRU cache keyed by (size, distance, wavelength, pitch), so recurring
+ * optics reuse them.  One request: */
+typedef struct ph_serve_request {
+    const float *hologram;   /* Float32 [n_slow][n_fast]; wavefront = sqrt(hologram) + 0i */
+    float *proj;             /* out: minimum over slices of |u|^2 */
+    int32_t *argmin;         /* out (nullable): first slice attaining it */
+    int32_t n_fast, n_slow, slices;
+    double z0, dz;           /* micrometres: first slice at z0, then steps of dz */
+    double wavlen, dx;       /* micrometres */
+} ph_serve_request;
+
+typedef struct ph_server ph_server;
+
+enum { PH_PENDING = 9 };   /* ph_serve_poll: the request has not finished */
+
+/* Creates a server for requests up to max_n_fast x max_n_slow x max_slices
+ * (reconstruction of holofunc.jl:248-266; allocates the lanes' scratch). */
+PH_API int32_t ph_serve_create(ph_ctx *ctx, int32_t lanes, int32_t max_n_fast, int32_t max_n_slow,
+                               int32_t max_slices, int32_t tf_cache_entries, ph_server **out);
+/* Queues one cu_get_reconst_xyprojection (holofunc.jl:248-266) request and
+ * returns at once with its ticket.  The request runs after the work already
+ * queued on `stream` (the one that wrote the hologram).  The hologram and
+ * outputs must stay valid until the request has finished.  Thread-safe; one
+ * poller per ticket. */
+PH_API int32_t ph_serve_submit(ph_server *srv, const ph_serve_request *req, int64_t *ticket, void *stream);
+/* PH_OK when the request has finished (the ticket is then released and
+ * *latency_ms, if non-NULL, is submission to completion), PH_PENDING if not yet
+ * (wait = 0), or waits for it (wait = 1).  No reference counterpart. */
+PH_API int32_t ph_serve_poll(ph_server *srv, int64_t ticket, int32_t wait, double *latency_ms);
+/* Waits for every request, frees the server (no reference counterpart). */
+PH_API void ph_serve_destroy(ph_server *srv);
+
 /* ---- synthetic input ----------------------------------------------------------- */
 
 /* No reference counterpart (the reference ships no generator): the seeded

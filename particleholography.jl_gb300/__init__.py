@@ -10,6 +10,7 @@ The directory name is not a Python identifier; load the package with
 """
 from . import _lib
 from .batch import ReconBatch
+from .serve import Server
 from .ccl import (count_labels, cu_bounding_rectangles, cu_connected_component_labeling,
                   cu_connected_component_labeling_batch, cu_find_valid_labels)
 from .frequency_filters import (cu_apply_low_pass_filter, cu_apply_low_pass_filter_, cu_rectangle_filter,

@@ -9,7 +9,12 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <map>
+#include <thread>
+#include <tuple>
+#include <unordered_map>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -18,6 +23,42 @@
 
 #include "ph_ctx.h"
 #include "ph_launch.cuh"
+
+// The serving runtime: lanes (stream + scratch), the transfer-function cache
+// and the tickets of requests in flight.
+struct ph_serve_ticket {
+    std::atomic<int> done{0};
+    double t_submit = 0.0, t_done = 0.0;   // seconds, steady clock
+    cudaEvent_t ev = nullptr;              // completes after the host callback ran
+    int lane = 0;
+    std::atomic<int> *lane_inflight = nullptr;
+};
+
+struct ph_serve_tf {
+    float2 *buf = nullptr;
+    cudaEvent_t ready = nullptr;      // the build finished
+    cudaEvent_t last_use = nullptr;   // the last request that read it finished
+    uint64_t stamp = 0;               // LRU order
+};
+
+struct ph_server {
+    ph_ctx *ctx = nullptr;
+    std::mutex mu;
+    int lanes = 1;
+    int max_nx = 0, max_ny = 0, max_slices = 0;
+    size_t lane_bytes = 0;
+    void *scratch = nullptr;               // lanes x lane_bytes (+ d_sqr buffers)
+    std::vector<cudaStream_t> streams;
+    std::vector<std::atomic<int>> inflight;
+    std::map<std::tuple<int, int, double, double, double>, ph_serve_tf> tfs;
+    int tf_cap = 16;
+    uint64_t clock = 0;
+    int64_t next_ticket = 1;
+    std::unordered_map<int64_t, ph_serve_ticket *> tickets;
+    std::vector<cudaEvent_t> event_pool;
+    cudaEvent_t order = nullptr;           // orders a lane after the submitting stream
+    explicit ph_server(int n) : inflight(n) {}
+};
 
 // A planned batch of reconstructions: its items, lanes, own scratch and the
 // recorded graph.
@@ -699,6 +740,76 @@ int issue_propagate(ph_ctx *ctx, float2 *out, const float2 *in, const float2 *h,
 
 // ---------------------------------------------------------------- batches
 
+// ---------------------------------------------------------------- serving
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+void CUDART_CB serve_done(void *p) {   // host callback: no CUDA calls here
+    auto *t = static_cast<ph_serve_ticket *>(p);
+    t->t_done = now_s();
+    t->lane_inflight->fetch_sub(1);
+    t->done.store(1, std::memory_order_release);
+}
+
+cudaEvent_t serve_event(ph_server *srv) {
+    if (!srv->event_pool.empty()) {
+        cudaEvent_t e = srv->event_pool.back();
+        srv->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+// The transfer function H(-z) of a request's grid, built on stream `ls` (the
+// reference's Float32 square-root term, then its FP64-phase exponential) or
+// taken from the cache; `ls` is ordered after its build.
+int serve_transfer(ph_server *srv, cudaStream_t ls, float *dsqr, int nx, int ny, double z, double wavlen,
+                   double dx, const float2 **out, ph_serve_tf **entry) {
+    ph_ctx *ctx = srv->ctx;
+    const auto key = std::make_tuple(nx, ny, z, wavlen, dx);
+    auto it = srv->tfs.find(key);
+    if (it == srv->tfs.end()) {
+        if ((int)srv->tfs.size() >= srv->tf_cap) {   // evict the least recently used entry
+            auto victim = srv->tfs.begin();
+            for (auto jt = srv->tfs.begin(); jt != srv->tfs.end(); ++jt)
+                if (jt->second.stamp < victim->second.stamp) victim = jt;
+            // requests on any lane may still read it: let every lane drain first (evictions are rare)
+            for (auto x : srv->streams) PH_CUDA(cudaStreamSynchronize(x), "cudaStreamSynchronize");
+            cudaFree(victim->second.buf);
+            cudaEventDestroy(victim->second.ready);
+            cudaEventDestroy(victim->second.last_use);
+            srv->tfs.erase(victim);
+        }
+        ph_serve_tf e{};
+        PH_CUDA(cudaMalloc(&e.buf, sizeof(float2) * (size_t)nx * ny), "cudaMalloc(transfer)");
+        if (cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&e.last_use, cudaEventDisableTiming) != cudaSuccess) {
+            cudaFree(e.buf);
+            return cuda_status(ctx, cudaGetLastError(), "cudaEventCreate");
+        }
+        dim3 b(32, 8);
+        k_transfer_sqrt<<<grid2d(nx, ny, b), b, 0, ls>>>(dsqr, nx, ny, wavlen, dx);
+        const size_t n = (size_t)nx * ny;
+        k_transfer<<<(unsigned)((n + 255) / 256), 256, 0, ls>>>(e.buf, dsqr, n, (2.0 * M_PI * (-z)) / wavlen);
+        PH_TRY(launched(ctx, cudaGetLastError(), "serve transfer", 2));
+        PH_CUDA(cudaEventRecord(e.ready, ls), "cudaEventRecord");
+        it = srv->tfs.emplace(key, e).first;
+    } else {
+        PH_CUDA(cudaStreamWaitEvent(ls, it->second.ready, 0), "cudaStreamWaitEvent");
+    }
+    it->second.stamp = ++srv->clock;
+    *out = it->second.buf;
+    *entry = &it->second;
+    return PH_OK;
+}
+
 // Longest-processing-time assignment of items (work = pixels x slices) to lanes.
 std::vector<int> assign_lanes(const ph_recon_item *items, int count, int lanes) {
     std::vector<int> order(count), lane(count, 0);
@@ -1302,6 +1413,182 @@ void ph_batch_destroy(ph_batch *batch) {
         cudaGetLastError();
     }
     delete batch;
+}
+
+int32_t ph_serve_create(ph_ctx *ctx, int32_t lanes, int32_t max_n_fast, int32_t max_n_slow, int32_t max_slices,
+                        int32_t tf_cache_entries, ph_server **out) {
+    PH_ENTER(ctx, nullptr);
+    PH_NONNULL(out, "out");
+    *out = nullptr;
+    if (lanes < 1 || lanes > 16) { set_err(ctx, "lanes must be in 1..16. Got %d.", lanes); return PH_ERR_INVALID; }
+    if (max_slices < 1) { set_err(ctx, "max_slices must be >= 1. Got %d.", max_slices); return PH_ERR_SIZE; }
+    if (tf_cache_entries < 2) { set_err(ctx, "the transfer cache needs at least 2 entries"); return PH_ERR_INVALID; }
+    PH_TRY(check_len(ctx, max_n_fast, max_n_slow));
+    auto *srv = new ph_server(lanes);
+    srv->ctx = ctx;
+    srv->lanes = lanes;
+    srv->max_nx = max_n_fast;
+    srv->max_ny = max_n_slow;
+    srv->max_slices = max_slices;
+    srv->tf_cap = tf_cache_entries;
+    const ReconLayout L = recon_layout(ctx, max_n_fast, max_n_slow, max_n_slow, max_n_fast, max_slices);
+    srv->lane_bytes = (L.total + kAlign - 1) / kAlign * kAlign +
+                      ((size_t)max_n_fast * max_n_slow * sizeof(float) + kAlign - 1) / kAlign * kAlign;
+    const size_t total = srv->lane_bytes * lanes;
+    auto fail = [&](int code) {
+        for (auto x : srv->streams) if (x) cudaStreamDestroy(x);
+        if (srv->order) cudaEventDestroy(srv->order);
+        if (srv->scratch) cudaFree(srv->scratch);
+        delete srv;
+        cudaGetLastError();
+        return code;
+    };
+    if (ctx->budget && total + ctx->scratch_bytes > ctx->budget) {
+        set_err(ctx, "server scratch of %zu bytes exceeds the context's HBM budget of %zu bytes", total, ctx->budget);
+        return fail(PH_ERR_OOM);
+    }
+    if (cudaMalloc(&srv->scratch, total) != cudaSuccess) {
+        set_err(ctx, "cudaMalloc of %zu bytes of server scratch failed", total);
+        return fail(PH_ERR_OOM);
+    }
+    srv->streams.assign(lanes, nullptr);
+    if (cudaEventCreateWithFlags(&srv->order, cudaEventDisableTiming) != cudaSuccess) return fail(PH_ERR_CUDA);
+    for (int l = 0; l < lanes; ++l) {
+        if (cudaStreamCreateWithFlags(&srv->streams[l], cudaStreamNonBlocking) != cudaSuccess) {
+            set_err(ctx, "could not create the server lanes");
+            return fail(PH_ERR_CUDA);
+        }
+    }
+    *out = srv;
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_serve_submit(ph_server *srv, const ph_serve_request *req, int64_t *ticket, void *stream) {
+    if (srv == nullptr || req == nullptr || ticket == nullptr) return PH_ERR_INVALID;
+    ph_ctx *ctx = srv->ctx;
+    std::lock_guard<std::mutex> slk(srv->mu);
+    std::lock_guard<std::mutex> clk(ctx->mu);
+    DeviceGuard dg(ctx->device);
+    const int nx = req->n_fast, ny = req->n_slow;
+    PH_NONNULL(req->hologram, "hologram");
+    if (req->proj == nullptr && req->argmin == nullptr) { set_err(ctx, "proj and argmin are both NULL"); return PH_ERR_INVALID; }
+    if (req->slices < 1) { set_err(ctx, "slices must be >= 1. Got %d.", req->slices); return PH_ERR_SIZE; }
+    PH_TRY(check_len(ctx, nx, ny));
+    const ReconLayout L = recon_layout(ctx, nx, ny, ny, nx, req->slices);
+    const size_t dsqr_off = srv->lane_bytes - ((size_t)srv->max_nx * srv->max_ny * sizeof(float) + kAlign - 1) / kAlign * kAlign;
+    if (L.total > dsqr_off || (size_t)nx * ny > (size_t)srv->max_nx * srv->max_ny) {
+        set_err(ctx, "request %d x %d x %d exceeds the server's maximum %d x %d x %d", nx, ny, req->slices,
+                srv->max_nx, srv->max_ny, srv->max_slices);
+        return PH_ERR_SIZE;
+    }
+    // the lane with the fewest requests in flight
+    int lane = 0;
+    for (int l = 1; l < srv->lanes; ++l)
+        if (srv->inflight[l].load() < srv->inflight[lane].load()) lane = l;
+    cudaStream_t ls = srv->streams[lane];
+    // after the work already queued on the caller's stream (which wrote the hologram)
+    PH_CUDA(cudaEventRecord(srv->order, static_cast<cudaStream_t>(stream)), "cudaEventRecord");
+    PH_CUDA(cudaStreamWaitEvent(ls, srv->order, 0), "cudaStreamWaitEvent");
+    char *base = static_cast<char *>(srv->scratch) + (size_t)lane * srv->lane_bytes;
+    const float2 *tw_x = nullptr, *tw_y = nullptr;
+    for (int n : {nx, ny}) {   // a new twiddle table is complete before any lane reads it
+        if (ctx->tw.find(n) == ctx->tw.end()) {
+            const float2 *tw = nullptr;
+            PH_TRY(get_twiddles(ctx, n, ls, &tw));
+            PH_CUDA(cudaStreamSynchronize(ls), "cudaStreamSynchronize");
+        }
+    }
+    tw_x = ctx->tw[nx];
+    tw_y = ctx->tw[ny];
+    const float2 *hf = nullptr, *hdz = nullptr;
+    ph_serve_tf *ef = nullptr, *ed = nullptr;
+    float *dsqr = reinterpret_cast<float *>(base + dsqr_off);
+    PH_TRY(serve_transfer(srv, ls, dsqr, nx, ny, req->z0, req->wavlen, req->dx, &hf, &ef));
+    PH_TRY(serve_transfer(srv, ls, dsqr, nx, ny, req->dz, req->wavlen, req->dx, &hdz, &ed));
+    auto *t = new ph_serve_ticket();
+    t->t_submit = now_s();
+    t->lane = lane;
+    t->lane_inflight = &srv->inflight[lane];
+    t->ev = serve_event(srv);
+    if (t->ev == nullptr) { delete t; set_err(ctx, "cudaEventCreate failed"); return PH_ERR_CUDA; }
+    auto *state = reinterpret_cast<float4 *>(base + L.state);
+    auto *p64 = reinterpret_cast<unsigned long long *>(base + L.p64);
+    int st = issue_spectrum(ctx, nullptr, hf, hdz, nx, ny, false, nx, ny, reinterpret_cast<float2 *>(base + L.a1),
+                            state, tw_x, tw_y, reinterpret_cast<double *>(base + L.acc),
+                            reinterpret_cast<float2 *>(base + L.mean), ls, req->hologram);
+    if (st == PH_OK && cudaMemsetAsync(p64, 0xff, sizeof(unsigned long long) * nx * ny, ls) != cudaSuccess)
+        st = cuda_status(ctx, cudaGetLastError(), "cudaMemsetAsync");
+    if (st == PH_OK)
+        st = issue_recon_slices(ctx, RK_PROJ, req->proj, req->argmin, nullptr, PH_F32, nx, ny, nx, ny, 0, 0,
+                                req->slices, L.batch, state, reinterpret_cast<float2 *>(base + L.t), p64, tw_x, tw_y,
+                                true, ls);
+    if (st != PH_OK) {
+        srv->event_pool.push_back(t->ev);
+        delete t;
+        return st;
+    }
+    cudaEventRecord(ef->last_use, ls);
+    cudaEventRecord(ed->last_use, ls);
+    srv->inflight[lane].fetch_add(1);
+    PH_CUDA(cudaLaunchHostFunc(ls, serve_done, t), "cudaLaunchHostFunc");
+    PH_CUDA(cudaEventRecord(t->ev, ls), "cudaEventRecord");
+    *ticket = srv->next_ticket++;
+    srv->tickets[*ticket] = t;
+    return PH_OK;
+}
+
+int32_t ph_serve_poll(ph_server *srv, int64_t ticket, int32_t wait, double *latency_ms) {
+    if (srv == nullptr) return PH_ERR_INVALID;
+    ph_serve_ticket *t = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        auto it = srv->tickets.find(ticket);
+        if (it == srv->tickets.end()) {
+            std::lock_guard<std::mutex> clk(srv->ctx->mu);
+            set_err(srv->ctx, "unknown ticket %lld", (long long)ticket);
+            return PH_ERR_INVALID;
+        }
+        t = it->second;
+        if (!t->done.load(std::memory_order_acquire) && !wait) return PH_PENDING;
+    }
+    if (!t->done.load(std::memory_order_acquire)) {
+        DeviceGuard dg(srv->ctx->device);
+        const cudaError_t e = cudaEventSynchronize(t->ev);   // recorded after the callback
+        if (e != cudaSuccess) {
+            std::lock_guard<std::mutex> clk(srv->ctx->mu);
+            return cuda_status(srv->ctx, e, "cudaEventSynchronize");
+        }
+    }
+    std::lock_guard<std::mutex> lk(srv->mu);
+    if (latency_ms) *latency_ms = (t->t_done - t->t_submit) * 1e3;
+    srv->event_pool.push_back(t->ev);
+    srv->tickets.erase(ticket);
+    delete t;
+    return PH_OK;
+}
+
+void ph_serve_destroy(ph_server *srv) {
+    if (srv == nullptr) return;
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        DeviceGuard dg(srv->ctx->device);
+        for (auto x : srv->streams) cudaStreamSynchronize(x);
+        for (auto &kv : srv->tickets) {
+            srv->event_pool.push_back(kv.second->ev);
+            delete kv.second;
+        }
+        for (auto e : srv->event_pool) cudaEventDestroy(e);
+        for (auto &kv : srv->tfs) {
+            cudaFree(kv.second.buf);
+            cudaEventDestroy(kv.second.ready);
+            cudaEventDestroy(kv.second.last_use);
+        }
+        for (auto x : srv->streams) cudaStreamDestroy(x);
+        if (srv->order) cudaEventDestroy(srv->order);
+        if (srv->scratch) cudaFree(srv->scratch);
+        cudaGetLastError();
+    }
+    delete srv;
 }
 
 int32_t ph_reconst_vol(ph_ctx *ctx, void *vol, int32_t vol_dtype, float *proj, const void *wf, const void *tf_front,
