@@ -18,7 +18,8 @@ export cu_transfer_sqrt_arr, cu_transfer, cu_gabor_wavefront, cu_phase_retrieval
        cu_get_reconst_xyprojection, cu_get_reconst_vol_and_xyprojection, cu_get_reconst_complex_vol,
        cu_asm_prop!, cu_2d_pad, cu_get_reconst_vol_and_xyprojection_padded,
        cu_connected_component_labeling, count_labels, cu_find_valid_labels,
-       cu_get_reconst_xyprojection_argmin, cu_apply_low_pass_filter!, cu_apply_low_pass_filter
+       cu_get_reconst_xyprojection_argmin, cu_apply_low_pass_filter!, cu_apply_low_pass_filter,
+       ReconBatch, run!, Server, submit!, poll
 
 const libphgb300 = get(ENV, "PHGB300_LIB", joinpath(@__DIR__, "..", "libphgb300.so"))
 
@@ -217,6 +218,113 @@ function cu_find_valid_labels(labels::CuArray{UInt32,2})
     c, _ = _roots(labels, 0)
     _, roots = _roots(labels, c)
     return roots[1:c]
+end
+
+# ---- batches and serving (no single reference counterpart) ------------------------
+
+# ph_recon_item (phgb300.h)
+struct _ReconItem
+    hologram::CuPtr{Float32}
+    wavefront::CuPtr{ComplexF32}
+    tf_front::CuPtr{ComplexF32}
+    tf_dz::CuPtr{ComplexF32}
+    proj::CuPtr{Float32}
+    argmin::CuPtr{Int32}
+    n_fast::Int32
+    n_slow::Int32
+    slices::Int32
+end
+
+# A batch of cu_get_reconst_xyprojection calls (holofunc.jl:248-266) recorded as
+# one CUDA graph; `items` are (hologram::CuArray{Float32,2}, transfer_front,
+# transfer_dz, slices) tuples.  The arrays must outlive the batch.
+mutable struct ReconBatch
+    handle::Ptr{Cvoid}
+    proj::Vector{CuArray{Float32,2}}
+    argmin::Vector{CuArray{Int32,2}}
+    keep::Vector{Any}
+end
+
+function ReconBatch(items; lanes::Int=4)
+    recs = _ReconItem[]
+    proj = CuArray{Float32,2}[]
+    amin = CuArray{Int32,2}[]
+    for (holo, tf, td, slices) in items
+        @assert size(holo) == size(tf.data) == size(td.data) "All arrays must have the same size. Got $(size(holo)), $(size(tf.data)), $(size(td.data))."
+        p = CuArray{Float32}(undef, size(holo)...)
+        a = CuArray{Int32}(undef, size(holo)...)
+        push!(proj, p); push!(amin, a)
+        push!(recs, _ReconItem(pointer(holo), CU_NULL, pointer(tf.data), pointer(td.data), pointer(p), pointer(a),
+                               size(holo, 1), size(holo, 2), slices))
+    end
+    CUDA.synchronize()
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    _check(ccall((:ph_batch_plan, libphgb300), Int32, (Ptr{Cvoid}, Ptr{_ReconItem}, Int32, Int32, Ref{Ptr{Cvoid}}),
+                 _ctx(), recs, length(recs), lanes, h))
+    b = ReconBatch(h[], proj, amin, Any[items])
+    finalizer(b) do x
+        x.handle == C_NULL || ccall((:ph_batch_destroy, libphgb300), Cvoid, (Ptr{Cvoid},), x.handle)
+    end
+    return b
+end
+
+function run!(b::ReconBatch)
+    _check(ccall((:ph_batch_run, libphgb300), Int32, (Ptr{Cvoid}, Ptr{Cvoid}), b.handle, _stream()))
+    return b.proj, b.argmin
+end
+
+# ph_serve_request (phgb300.h)
+struct _ServeRequest
+    hologram::CuPtr{Float32}
+    proj::CuPtr{Float32}
+    argmin::CuPtr{Int32}
+    n_fast::Int32
+    n_slow::Int32
+    slices::Int32
+    z0::Float64
+    dz::Float64
+    wavlen::Float64
+    dx::Float64
+end
+
+mutable struct Server
+    handle::Ptr{Cvoid}
+    live::Dict{Int64,Any}
+end
+
+function Server(max_size::Tuple{Int,Int}, max_slices::Int; lanes::Int=3, tf_cache::Int=16)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    _check(ccall((:ph_serve_create, libphgb300), Int32,
+                 (Ptr{Cvoid}, Int32, Int32, Int32, Int32, Int32, Ref{Ptr{Cvoid}}),
+                 _ctx(), lanes, max_size[1], max_size[2], max_slices, tf_cache, h))
+    s = Server(h[], Dict{Int64,Any}())
+    finalizer(s) do x
+        x.handle == C_NULL || ccall((:ph_serve_destroy, libphgb300), Cvoid, (Ptr{Cvoid},), x.handle)
+    end
+    return s
+end
+
+# Queues the projection of `holo` into `proj` (and `argmin`); returns a ticket.
+function submit!(s::Server, holo::CuArray{Float32,2}, proj::CuArray{Float32,2}, slices::Int, z0::Real, dz::Real;
+                 wavlen::Real=0.6328, dx::Real=10.0, argmin::Union{Nothing,CuArray{Int32,2}}=nothing)
+    req = Ref(_ServeRequest(pointer(holo), pointer(proj), argmin === nothing ? CU_NULL : pointer(argmin),
+                            size(holo, 1), size(holo, 2), slices, z0, dz, wavlen, dx))
+    t = Ref{Int64}(0)
+    _check(ccall((:ph_serve_submit, libphgb300), Int32, (Ptr{Cvoid}, Ref{_ServeRequest}, Ref{Int64}, Ptr{Cvoid}),
+                 s.handle, req, t, _stream()))
+    s.live[t[]] = (holo, proj, argmin)
+    return t[]
+end
+
+# The request's latency in ms once finished, `nothing` while pending.
+function poll(s::Server, ticket::Int64; wait::Bool=false)
+    lat = Ref{Float64}(0.0)
+    st = ccall((:ph_serve_poll, libphgb300), Int32, (Ptr{Cvoid}, Int64, Int32, Ref{Float64}), s.handle, ticket,
+               wait ? 1 : 0, lat)
+    st == Int32(9) && return nothing
+    _check(st)
+    delete!(s.live, ticket)
+    return lat[]
 end
 
 end # module
