@@ -174,6 +174,15 @@ PH_API int32_t ph_reconst_xyproj(ph_ctx *ctx, float *proj, int32_t *argmin, cons
                           const void *tf_front, const void *tf_dz,
                           int32_t n_fast, int32_t n_slow, int32_t slices, void *stream);
 
+/* cu_apply_low_pass_filter (frequency_filters.jl:88-107) followed by
+ * cu_get_reconst_xyprojection (holofunc.jl:248-266), with the filter folded
+ * into the spectrum: X_k = fftshift(fft(wf)) .* lpf .* tf_front .* tf_dz^k, no
+ * inverse/forward FFT pair.  lpf: Float32 centred [n_slow][n_fast] (the
+ * reference's CuLowPassFilter). */
+PH_API int32_t ph_reconst_xyproj_lpf(ph_ctx *ctx, float *proj, int32_t *argmin, const void *wf,
+                                     const void *tf_front, const void *tf_dz, const float *lpf,
+                                     int32_t n_fast, int32_t n_slow, int32_t slices, void *stream);
+
 /* cu_get_reconst_vol (holofunc.jl:184-200, vol_dtype N0F8/F16/F32/F64),
  * cu_get_reconst_complex_vol (holofunc.jl:216-232, vol_dtype C64) and
  * cu_get_reconst_vol_and_xyprojection (holofunc.jl:300-321, proj non-null:
@@ -181,6 +190,15 @@ PH_API int32_t ph_reconst_xyproj(ph_ctx *ctx, float *proj, int32_t *argmin, cons
 PH_API int32_t ph_reconst_vol(ph_ctx *ctx, void *vol, int32_t vol_dtype, float *proj, const void *wf,
                        const void *tf_front, const void *tf_dz,
                        int32_t n_fast, int32_t n_slow, int32_t slices, void *stream);
+
+/* The binary volume particle_bounding_boxes consumes (particle_detection.jl:58-76):
+ * vol[k][y][x] = clamp(|slice_k|^2, 0, 1) <= threshold as Bool (UInt8 0/1),
+ * i.e. cu_get_reconst_vol(..., Float32) (holofunc.jl:184-200) .<= threshold in
+ * one pass, without storing the Float32 volume.  proj (nullable): the strict-<
+ * minimum of the clamped intensities, as ph_reconst_vol with F32. */
+PH_API int32_t ph_reconst_binary_vol(ph_ctx *ctx, uint8_t *vol, float threshold, float *proj, const void *wf,
+                                     const void *tf_front, const void *tf_dz, int32_t n_fast, int32_t n_slow,
+                                     int32_t slices, void *stream);
 
 /* cu_get_reconst_vol_and_xyprojection_padded (holofunc.jl:339-364): wf is
  * n x n, the transfer functions 2n x 2n; vol is N0f8 n x n x slices (the centre

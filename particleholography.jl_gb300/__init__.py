@@ -10,6 +10,7 @@ The directory name is not a Python identifier; load the package with
 """
 from . import _lib
 from .batch import ReconBatch
+from .detection import cu_get_reconst_binary_vol, slice_bounding_boxes
 from .serve import Server
 from .ccl import (count_labels, cu_bounding_rectangles, cu_connected_component_labeling,
                   cu_connected_component_labeling_batch, cu_find_valid_labels)
@@ -17,7 +18,7 @@ from .frequency_filters import (cu_apply_low_pass_filter, cu_apply_low_pass_filt
                                 cu_super_gaussian_filter)
 from .holofunc import (cu_2d_pad, cu_asm_prop_, cu_gabor_wavefront, cu_get_reconst_complex_vol,
                        cu_get_reconst_vol, cu_get_reconst_vol_and_xyprojection,
-                       cu_get_reconst_vol_and_xyprojection_padded, cu_get_reconst_xyprojection,
+                       cu_get_reconst_vol_and_xyprojection_padded, cu_get_reconst_xyprojection, cu_get_reconst_xyprojection_lpf,
                        cu_phase_retrieval_holo, cu_transfer, cu_transfer_fp64, cu_transfer_sqrt_arr)
 from .types import CuLowPassFilter, CuTransfer, CuTransferSqrtPart, CuWavefront, N0f8
 

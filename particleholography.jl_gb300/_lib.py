@@ -58,6 +58,8 @@ SIGNATURES = {
     "ph_phase_retrieval": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp]),
     "ph_asm_prop": (_i32, [_vp, _vp, _vp, _vp, _f64, _i32, _i32, _f64, _vp]),
     "ph_reconst_xyproj": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
+    "ph_reconst_xyproj_lpf": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
+    "ph_reconst_binary_vol": (_i32, [_vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "ph_reconst_vol": (_i32, [_vp, _vp, _i32, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "ph_reconst_vol_padded": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "ph_propagate": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _vp]),

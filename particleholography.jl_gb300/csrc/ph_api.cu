@@ -532,7 +532,8 @@ struct Spectrum {
 // NULL) the wavefront is sqrt(holo) + 0i, formed in the first FFT stage.
 int issue_spectrum(ph_ctx *ctx, const float2 *wf, const float2 *hf, const float2 *hdz, int nx, int ny,
                    bool padded, int nin_x, int nin_y, float2 *a1, float4 *state, const float2 *tw_x,
-                   const float2 *tw_y, double *acc, float2 *mean, cudaStream_t s, const float *holo = nullptr) {
+                   const float2 *tw_y, double *acc, float2 *mean, cudaStream_t s, const float *holo = nullptr,
+                   const float *lpf = nullptr) {
     if (holo != nullptr) {
         FwdRowsT<FWD_SQRT_REAL> f{};
         f.src_real = holo;
@@ -567,6 +568,7 @@ int issue_spectrum(ph_ctx *ctx, const float2 *wf, const float2 *hf, const float2
     c.a1 = a1;
     c.hf = hf;
     c.hdz = hdz;
+    c.lpf = lpf;
     c.state = state;
     c.tw = tw_y;
     c.nx = nx;
@@ -609,12 +611,12 @@ enum ReconKind { RK_PROJ, RK_VOL, RK_CVOL, RK_PADDED };
 int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype, int nx,
                        int ny, int nx_out, int ny_out, int x0, int y0, int slices, int batch, float4 *state, float2 *t,
                        unsigned long long *p64, const float2 *tw_x, const float2 *tw_y, bool want_proj,
-                       cudaStream_t s);
+                       cudaStream_t s, float threshold = 0.0f);
 
 // Shared driver of every reconstruction entry point.
 int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype,
                 const float2 *wf, const float2 *hf, const float2 *hdz, int nin_x, int nin_y, int slices,
-                cudaStream_t s) {
+                cudaStream_t s, const float *lpf = nullptr, float threshold = 0.0f) {
     const bool padded = kind == RK_PADDED;
     const int nx = padded ? 2 * nin_x : nin_x;
     const int ny = padded ? 2 * nin_y : nin_y;
@@ -632,15 +634,17 @@ int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void 
     float2 *t = at<float2>(ctx, L.t);
     const bool want_proj = (kind == RK_PROJ) || proj != nullptr || argmin != nullptr;
     char key[512];
-    snprintf(key, sizeof key, "recon|%d|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%d", (int)kind, nin_x, nin_y, slices,
-             L.batch, vol_dtype, (void *)proj, (void *)argmin, vol, (const void *)wf, (const void *)hf,
-             (const void *)hdz, ctx->scratch, (int)ctx->opt_loop_limit);
+    uint32_t thr_bits = 0;
+    memcpy(&thr_bits, &threshold, sizeof thr_bits);
+    snprintf(key, sizeof key, "recon|%d|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%d|%p|%08x", (int)kind, nin_x, nin_y,
+             slices, L.batch, vol_dtype, (void *)proj, (void *)argmin, vol, (const void *)wf, (const void *)hf,
+             (const void *)hdz, ctx->scratch, (int)ctx->opt_loop_limit, (const void *)lpf, thr_bits);
     return run_graph(ctx, s, key, [&](cudaStream_t s) -> int {
         PH_TRY(issue_spectrum(ctx, wf, hf, hdz, nx, ny, padded, nin_x, nin_y, at<float2>(ctx, L.a1), state, tw_x,
-                              tw_y, at<double>(ctx, L.acc), at<float2>(ctx, L.mean), s));
+                              tw_y, at<double>(ctx, L.acc), at<float2>(ctx, L.mean), s, nullptr, lpf));
         if (want_proj) PH_CUDA(cudaMemsetAsync(p64, 0xff, sizeof(unsigned long long) * nx_out * ny_out, s), "memset");
         return issue_recon_slices(ctx, kind, proj, argmin, vol, vol_dtype, nx, ny, nx_out, ny_out, x0, y0, slices,
-                                  L.batch, state, t, p64, tw_x, tw_y, want_proj, s);
+                                  L.batch, state, t, p64, tw_x, tw_y, want_proj, s, threshold);
     });
 }
 
@@ -661,7 +665,7 @@ int recon_group(int nbatch, int nx_rows_a) {
 int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype, int nx,
                        int ny, int nx_out, int ny_out, int x0, int y0, int slices, int batch, float4 *state, float2 *t,
                        unsigned long long *p64, const float2 *tw_x, const float2 *tw_y, bool want_proj,
-                       cudaStream_t s) {
+                       cudaStream_t s, float threshold) {
     ReconLayout L{};
     L.batch = batch;
     const int row_blocks_a = (nx + recon_a_rows(ny) - 1) / recon_a_rows(ny);
@@ -695,6 +699,7 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
         } else {
             ReconB<EPI_VOL> b{};
             b.t = t; b.tw = tw_x; b.vol = vol; b.vol_dtype = vol_dtype; b.proj64 = want_proj ? p64 : nullptr;
+            b.threshold = threshold;
             b.rows = ny_out; b.nx_out = nx_out; b.x0 = x0;
             b.k0 = k0; b.nbatch = nb; b.group = group; b.vol_slice_stride = (long long)nx_out * ny_out;
             b.err = static_cast<int *>(ctx->small);
@@ -1591,6 +1596,22 @@ void ph_serve_destroy(ph_server *srv) {
     delete srv;
 }
 
+int32_t ph_reconst_xyproj_lpf(ph_ctx *ctx, float *proj, int32_t *argmin, const void *wf, const void *tf_front,
+                              const void *tf_dz, const float *lpf, int32_t n_fast, int32_t n_slow, int32_t slices,
+                              void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(wf, "wavefront");
+    PH_NONNULL(tf_front, "transfer_front");
+    PH_NONNULL(tf_dz, "transfer_dz");
+    PH_NONNULL(lpf, "lpf");
+    if (proj == nullptr && argmin == nullptr) { set_err(ctx, "proj and argmin are both NULL"); return PH_ERR_INVALID; }
+    if (slices < 1) { set_err(ctx, "slices must be >= 1. Got %d.", slices); return PH_ERR_SIZE; }
+    PH_TRY(reconstruct(ctx, RK_PROJ, proj, argmin, nullptr, PH_F32, static_cast<const float2 *>(wf),
+                       static_cast<const float2 *>(tf_front), static_cast<const float2 *>(tf_dz), n_fast, n_slow,
+                       slices, s, lpf));
+    PH_LEAVE(ctx);
+}
+
 int32_t ph_reconst_vol(ph_ctx *ctx, void *vol, int32_t vol_dtype, float *proj, const void *wf, const void *tf_front,
                        const void *tf_dz, int32_t n_fast, int32_t n_slow, int32_t slices, void *stream) {
     PH_ENTER(ctx, stream);
@@ -1610,6 +1631,21 @@ int32_t ph_reconst_vol(ph_ctx *ctx, void *vol, int32_t vol_dtype, float *proj, c
     PH_TRY(reconstruct(ctx, vol_dtype == PH_C64 ? RK_CVOL : RK_VOL, proj, nullptr, vol, vol_dtype,
                        static_cast<const float2 *>(wf), static_cast<const float2 *>(tf_front),
                        static_cast<const float2 *>(tf_dz), n_fast, n_slow, slices, s));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_reconst_binary_vol(ph_ctx *ctx, uint8_t *vol, float threshold, float *proj, const void *wf,
+                              const void *tf_front, const void *tf_dz, int32_t n_fast, int32_t n_slow, int32_t slices,
+                              void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(vol, "vol");
+    PH_NONNULL(wf, "wavefront");
+    PH_NONNULL(tf_front, "transfer_front");
+    PH_NONNULL(tf_dz, "transfer_dz");
+    if (slices < 1) { set_err(ctx, "slices must be >= 1. Got %d.", slices); return PH_ERR_SIZE; }
+    PH_TRY(reconstruct(ctx, RK_VOL, proj, nullptr, vol, PH_BOOL, static_cast<const float2 *>(wf),
+                       static_cast<const float2 *>(tf_front), static_cast<const float2 *>(tf_dz), n_fast, n_slow,
+                       slices, s, nullptr, threshold));
     PH_LEAVE(ctx);
 }
 

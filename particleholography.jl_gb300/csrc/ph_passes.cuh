@@ -177,6 +177,7 @@ __device__ __forceinline__ uint32_t phase_turns_u32(float2 h) {
 struct SpectrumCols : PassBase {
     const float2 *a1;        // [nx][ny]
     const float2 *hf, *hdz;  // centred [ny][nx]
+    const float *lpf;        // centred [ny][nx] low-pass filter, or null
     float4 *state;           // [nx][ny]
     const float2 *tw;
     int nx, ny;
@@ -194,7 +195,7 @@ struct SpectrumCols : PassBase {
             [&](int, int ky, float2 v) {
                 if (!valid) return;
                 const size_t c = (size_t)shift_idx(ky, N) * nx + sx;
-                const float2 x0 = cscale(cmul(v, hf[c]), scale);
+                const float2 x0 = cscale(cmul(v, hf[c]), lpf != nullptr ? scale * lpf[c] : scale);
                 const float2 d = hdz[c];
                 const float mag_m1 = (float)(sqrt((double)d.x * d.x + (double)d.y * d.y) - 1.0);
                 state[(size_t)kx * N + ky] = make_float4(x0.x, x0.y, __uint_as_float(phase_turns_u32(d)), mag_m1);
@@ -366,7 +367,8 @@ struct ReconB : PassBase {
     unsigned long long *proj64;      // [rows_out][nx_out] or null
     void *vol;                       // [S][rows_out][nx_out] or null
     int *err;                        // raised if a bulk-copy wait times out
-    int vol_dtype;
+    int vol_dtype;                   // PH_N0F8 .. PH_F64, or PH_BOOL: intensity <= threshold
+    float threshold;
     int rows;                        // rows of T per slice
     int nx_out, x0;                  // stored columns [x0, x0 + nx_out)
     int k0, nbatch, group;
@@ -471,6 +473,10 @@ struct ReconB : PassBase {
                                 }
                                 case 3:
                                     reinterpret_cast<double *>(vol)[o] = (double)i2;
+                                    stored = i2;
+                                    break;
+                                case 5:   // binary volume: the clamped Float32 intensity <= threshold
+                                    reinterpret_cast<uint8_t *>(vol)[o] = i2 <= threshold ? 1 : 0;
                                     stored = i2;
                                     break;
                                 default:

@@ -195,6 +195,25 @@ def cu_get_reconst_xyprojection(wavefront: CuWavefront, transfer_front: CuTransf
     return (proj, arg) if return_argmin else proj
 
 
+def cu_get_reconst_xyprojection_lpf(wavefront: CuWavefront, transfer_front: CuTransfer, transfer_dz: CuTransfer,
+                                    lpf, slices: int, return_argmin: bool = False):
+    """``cu_apply_low_pass_filter`` (frequency_filters.jl:88-107) then
+    ``cu_get_reconst_xyprojection`` (holofunc.jl:248-266) in one call: the
+    filter multiplies the spectrum the reconstruction already forms, so the
+    filter's own inverse/forward FFT pair disappears."""
+    wf, tf, td = _recon_args(wavefront, transfer_front, transfer_dz)
+    _check_same(wf, tf, td)
+    m = _need(_data(lpf), torch.float32, "lpf")
+    if tuple(m.shape) != tuple(wf.shape):
+        raise AssertionError(f"All arrays must have the same size. Got {_jsize(wf)}, {_jsize(m)}.")
+    proj = torch.empty(wf.shape, dtype=torch.float32, device=wf.device)
+    arg = torch.empty(wf.shape, dtype=torch.int32, device=wf.device) if return_argmin else None
+    ctx, s = _ctx_stream(wf)
+    ctx.call("ph_reconst_xyproj_lpf", proj.data_ptr(), arg.data_ptr() if arg is not None else None, wf.data_ptr(),
+             tf.data_ptr(), td.data_ptr(), m.data_ptr(), int(wf.shape[1]), int(wf.shape[0]), int(slices), s)
+    return (proj, arg) if return_argmin else proj
+
+
 def _reconst_vol(wavefront, transfer_front, transfer_dz, slices, return_type, with_proj):
     wf, tf, td = _recon_args(wavefront, transfer_front, transfer_dz)
     _check_same(wf, tf, td)

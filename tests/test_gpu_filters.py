@@ -44,3 +44,21 @@ def test_apply_matches_oracle(ph, cuda):
     m = ref.super_gaussian_filter(20000.0, 0.6328, n, 10.0)
     got = ph.cu_apply_low_pass_filter(ph.CuWavefront(to_dev(u, cuda)), ph.CuLowPassFilter(to_dev(m, cuda)))
     assert rel_l2(to_np(got.data), ref.apply_low_pass_filter(u, m)) < REL_L2
+
+
+@pytest.mark.parametrize("n,slices,build", [(256, 9, "super_gaussian"), (512, 5, "rectangle")])
+def test_filtered_projection_matches_filter_then_reconstruct(ph, cuda, n, slices, build):
+    """The low-pass filter folded into the reconstruction spectrum equals
+    cu_apply_low_pass_filter followed by cu_get_reconst_xyprojection."""
+    rng = np.random.default_rng(n)
+    holo = rng.uniform(0.1, 1.0, (n, n)).astype(np.float32)
+    d = ref.transfer_sqrt_arr(n, 0.6328, 10.0)
+    hf, hdz = ref.transfer(-3000.0, n, 0.6328, d), ref.transfer(-150.0, n, 0.6328, d)
+    mask = (ref.super_gaussian_filter if build == "super_gaussian" else ref.rectangle_filter)(60000.0, 0.6328, n, 10.0)
+    wf = ref.gabor_wavefront(holo)
+    want, want_arg = ref.reconst_xyprojection(ref.apply_low_pass_filter(wf, mask), hf, hdz, slices, with_argmin=True)
+    got, arg = ph.cu_get_reconst_xyprojection_lpf(ph.CuWavefront(to_dev(wf, cuda)), ph.CuTransfer(to_dev(hf, cuda)),
+                                                  ph.CuTransfer(to_dev(hdz, cuda)), to_dev(mask, cuda), slices,
+                                                  return_argmin=True)
+    assert rel_l2(to_np(got), want) < REL_L2
+    assert np.mean(to_np(arg) == want_arg) >= 0.999
