@@ -285,6 +285,25 @@ PH_API int32_t ph_serve_poll(ph_server *srv, int64_t ticket, int32_t wait, doubl
 /* Waits for every request, frees the server (no reference counterpart). */
 PH_API void ph_serve_destroy(ph_server *srv);
 
+/* ---- preprocessing ------------------------------------------------------------- */
+
+/* cu_make_background_mode (utils.jl:279-317) and make_background(...; mode=:mode)
+ * (utils.jl:210-231): the per-pixel most frequent value over `count` UInt8
+ * images ([count][n_slow][n_fast], device), the first maximum on ties, written
+ * as Float64 value / 255.  count <= 65535 (PH_ERR_TOO_LARGE beyond). */
+PH_API int32_t ph_background_mode(ph_ctx *ctx, double *out, const uint8_t *images, int64_t count, int32_t n_fast,
+                                  int32_t n_slow, void *stream);
+/* make_background(...; mode=:mean) (utils.jl:212-218): the per-pixel mean of
+ * the images read as Float32(value / 255), accumulated in Float64 in image order. */
+PH_API int32_t ph_background_mean(ph_ctx *ctx, double *out, const uint8_t *images, int64_t count, int32_t n_fast,
+                                  int32_t n_slow, void *stream);
+/* pad_with_mean (utils.jl:319-325): out (padsize x padsize Float32) = mean(img)
+ * (accumulated in Float64), with img (n_slow x n_fast) at fast offset
+ * padsize/2 - n_fast/2 and slow offset padsize/2 - n_slow/2.  padsize must
+ * exceed both sizes (the reference's @assert). */
+PH_API int32_t ph_pad_with_mean(ph_ctx *ctx, float *out, const float *img, int32_t n_fast, int32_t n_slow,
+                                int32_t padsize, void *stream);
+
 /* ---- synthetic input ----------------------------------------------------------- */
 
 /* No reference counterpart (the reference ships no generator): the seeded

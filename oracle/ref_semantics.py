@@ -356,3 +356,40 @@ def find_valid_labels(labels: np.ndarray) -> np.ndarray:
     ``i`` with ``labels[i] == i`` (the component roots), as Int64."""
     flat = np.asarray(labels).reshape(-1).astype(np.int64)
     return (np.nonzero(flat == np.arange(1, flat.size + 1, dtype=np.int64))[0] + 1).astype(np.int64)
+
+
+# ---------------------------------------------------------------- preprocessing (utils.jl)
+
+def make_background_mode(images) -> np.ndarray:
+    """``cu_make_background_mode`` (utils.jl:279-317) and ``make_background(...;
+    mode=:mode)`` (utils.jl:210-231): per-pixel most frequent UInt8 value over a
+    stack of images (votes per value, the first maximum on ties), / 255 as Float64."""
+    stack = np.asarray(images, dtype=np.uint8)
+    votes = np.zeros((256,) + stack.shape[1:], dtype=np.int64)
+    for img in stack:
+        np.add.at(votes, (img.astype(np.int64),) + tuple(np.indices(img.shape)), 1)
+    return np.argmax(votes, axis=0).astype(np.float64) / 255.0
+
+
+def make_background_mean(images) -> np.ndarray:
+    """``make_background(...; mode=:mean)`` (utils.jl:212-218): the mean of the
+    images as Float64, each UInt8 image read as Float32(value / 255)
+    (load_gray2float) and summed in image order."""
+    stack = (np.asarray(images, dtype=np.uint8).astype(np.float32) / np.float32(255.0)).astype(np.float64)
+    acc = np.zeros(stack.shape[1:], dtype=np.float64)
+    for img in stack:          # in image order, as the reference's loop
+        acc += img
+    return acc / len(stack)
+
+
+def pad_with_mean(img: np.ndarray, padsize: int) -> np.ndarray:
+    """``pad_with_mean`` (utils.jl:319-325) on a Julia ``(h, w)`` image held here as
+    ``(w, h)`` = ``(n_slow, n_fast)``: a padsize x padsize array of mean(img) with
+    the image at Julia rows ``div(p,2)-div(h,2)+1 ..`` and columns
+    ``div(p,2)-div(w,2)+1 ..``."""
+    n_slow, n_fast = img.shape
+    assert padsize > n_fast and padsize > n_slow, "Padsize should be larger than the image size."
+    out = np.full((padsize, padsize), np.float32(np.mean(img, dtype=np.float64)), dtype=np.float32)
+    o_fast, o_slow = padsize // 2 - n_fast // 2, padsize // 2 - n_slow // 2
+    out[o_slow:o_slow + n_slow, o_fast:o_fast + n_fast] = img
+    return out

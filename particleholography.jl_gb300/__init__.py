@@ -20,6 +20,7 @@ from .holofunc import (cu_2d_pad, cu_asm_prop_, cu_gabor_wavefront, cu_get_recon
                        cu_get_reconst_vol, cu_get_reconst_vol_and_xyprojection,
                        cu_get_reconst_vol_and_xyprojection_padded, cu_get_reconst_xyprojection, cu_get_reconst_xyprojection_lpf,
                        cu_phase_retrieval_holo, cu_transfer, cu_transfer_fp64, cu_transfer_sqrt_arr)
+from .utils import cu_make_background_mode, make_background, pad_with_mean
 from .types import CuLowPassFilter, CuTransfer, CuTransferSqrtPart, CuWavefront, N0f8
 
 LIB_PATH = _lib.LIB_PATH

@@ -81,6 +81,9 @@ SIGNATURES = {
     "ph_serve_submit": (_i32, [_vp, _vp, ctypes.POINTER(_i64), _vp]),
     "ph_serve_poll": (_i32, [_vp, _i64, _i32, ctypes.POINTER(_f64)]),
     "ph_serve_destroy": (None, [_vp]),
+    "ph_background_mode": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
+    "ph_background_mean": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
+    "ph_pad_with_mean": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp]),
 }
 
 PH_PENDING = 9

@@ -201,6 +201,71 @@ __global__ void k_pad_fill(float2 *out, const float2 *in, const float2 *mean, in
     out[(size_t)y * nout + x] = v;
 }
 
+// ---- preprocessing (utils.jl)
+
+// Per-pixel most frequent UInt8 value over `count` images (utils.jl:279-317):
+// each thread owns one pixel and its 256 vote counters in shared memory
+// ([bin][thread], so a warp's counters sit on distinct banks); the first
+// maximum wins, as the reference's argmax loop.
+constexpr int kModeThreads = 64;
+__global__ void __launch_bounds__(kModeThreads)
+    k_background_mode(double *out, const uint8_t *__restrict__ images, int64_t count, int64_t npix) {
+    __shared__ uint16_t hist[256][kModeThreads];
+    const int t = threadIdx.x;
+    const int64_t p = (int64_t)blockIdx.x * kModeThreads + t;
+    for (int b = 0; b < 256; ++b) hist[b][t] = 0;
+    if (p >= npix) return;
+    int64_t i = 0;
+    for (; i + 4 <= count; i += 4) {   // four independent loads in flight
+        const uint8_t v0 = images[(i + 0) * npix + p], v1 = images[(i + 1) * npix + p];
+        const uint8_t v2 = images[(i + 2) * npix + p], v3 = images[(i + 3) * npix + p];
+        ++hist[v0][t];
+        ++hist[v1][t];
+        ++hist[v2][t];
+        ++hist[v3][t];
+    }
+    for (; i < count; ++i) ++hist[images[i * npix + p]][t];
+    int best = 0;
+    uint16_t bc = hist[0][t];
+    for (int b = 1; b < 256; ++b) {
+        const uint16_t c = hist[b][t];
+        if (c > bc) { bc = c; best = b; }
+    }
+    out[p] = (double)best / 255.0;
+}
+
+// make_background(...; mode=:mean) (utils.jl:212-218): sum over the images of
+// Float64(Float32(q / 255)), in image order, over the count.
+__global__ void k_background_mean(double *out, const uint8_t *__restrict__ images, int64_t count, int64_t npix) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    double acc = 0.0;
+    for (int64_t i = 0; i < count; ++i) acc += (double)__fdiv_rn((float)images[i * npix + p], 255.0f);
+    out[p] = acc / (double)count;
+}
+
+__global__ void k_sum_f32(const float *in, size_t n, double *acc) {
+    double sx = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        sx += in[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sx += __shfl_xor_sync(0xffffffffu, sx, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(acc, sx);
+}
+
+// pad_with_mean (utils.jl:319-325): padsize^2 of mean(img), the image at fast /
+// slow offsets off_f / off_s.
+__global__ void k_pad_mean_fill(float *out, const float *in, const double *acc, double n, int nin_f, int nin_s,
+                                int pad, int off_f, int off_s) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= pad || y >= pad) return;
+    const int xi = x - off_f, yi = y - off_s;
+    float v = (float)(acc[0] / n);
+    if (xi >= 0 && xi < nin_f && yi >= 0 && yi < nin_s) v = in[(size_t)yi * nin_f + xi];
+    out[(size_t)y * pad + x] = v;
+}
+
 __global__ void k_proj_finish(const unsigned long long *p64, float *proj, int32_t *argmin, size_t n) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -1646,6 +1711,53 @@ int32_t ph_reconst_binary_vol(ph_ctx *ctx, uint8_t *vol, float threshold, float 
     PH_TRY(reconstruct(ctx, RK_VOL, proj, nullptr, vol, PH_BOOL, static_cast<const float2 *>(wf),
                        static_cast<const float2 *>(tf_front), static_cast<const float2 *>(tf_dz), n_fast, n_slow,
                        slices, s, nullptr, threshold));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_background_mode(ph_ctx *ctx, double *out, const uint8_t *images, int64_t count, int32_t n_fast,
+                           int32_t n_slow, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(images, "images");
+    if (count < 1 || n_fast < 1 || n_slow < 1) { set_err(ctx, "need at least one image of positive size"); return PH_ERR_SIZE; }
+    if (count > 65535) { set_err(ctx, "at most 65535 images per call. Got %lld.", (long long)count); return PH_ERR_TOO_LARGE; }
+    const int64_t npix = (int64_t)n_fast * n_slow;
+    k_background_mode<<<(unsigned)((npix + kModeThreads - 1) / kModeThreads), kModeThreads, 0, s>>>(out, images, count,
+                                                                                                    npix);
+    PH_TRY(launched(ctx, cudaGetLastError(), "background mode"));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_background_mean(ph_ctx *ctx, double *out, const uint8_t *images, int64_t count, int32_t n_fast,
+                           int32_t n_slow, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(images, "images");
+    if (count < 1 || n_fast < 1 || n_slow < 1) { set_err(ctx, "need at least one image of positive size"); return PH_ERR_SIZE; }
+    const int64_t npix = (int64_t)n_fast * n_slow;
+    k_background_mean<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(out, images, count, npix);
+    PH_TRY(launched(ctx, cudaGetLastError(), "background mean"));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_pad_with_mean(ph_ctx *ctx, float *out, const float *img, int32_t n_fast, int32_t n_slow, int32_t padsize,
+                         void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(out, "out");
+    PH_NONNULL(img, "img");
+    if (!(padsize > n_fast && padsize > n_slow) || n_fast < 1 || n_slow < 1) {
+        set_err(ctx, "Padsize should be larger than the image size. padsize: %d, img size: (%d, %d)", padsize, n_fast,
+                n_slow);
+        return PH_ERR_SIZE;
+    }
+    double *acc = reinterpret_cast<double *>(static_cast<char *>(ctx->small) + 64);
+    PH_CUDA(cudaMemsetAsync(acc, 0, sizeof(double), s), "cudaMemsetAsync");
+    const size_t n = (size_t)n_fast * n_slow;
+    k_sum_f32<<<256, 256, 0, s>>>(img, n, acc);
+    dim3 b(32, 8);
+    k_pad_mean_fill<<<grid2d(padsize, padsize, b), b, 0, s>>>(out, img, acc, (double)n, n_fast, n_slow, padsize,
+                                                             padsize / 2 - n_fast / 2, padsize / 2 - n_slow / 2);
+    PH_TRY(launched(ctx, cudaGetLastError(), "pad with mean", 2));
     PH_LEAVE(ctx);
 }
 

@@ -145,3 +145,28 @@ def test_gs_residual_decreases():
     _, r1 = ref.phase_retrieval_holo(h1, h2, tp, tpi, 1, n, return_residual=True)
     _, r10 = ref.phase_retrieval_holo(h1, h2, tp, tpi, 10, n, return_residual=True)
     assert r10 < r1
+
+
+def test_background_mode_first_maximum():
+    """cu_make_background_mode (utils.jl:279-317): the argmax loop keeps the first
+    (smallest) value among equally frequent ones."""
+    imgs = np.array([[[3, 1]], [[1, 1]], [[3, 2]], [[1, 2]]], dtype=np.uint8)   # pixel 0: 1 and 3 twice each
+    got = ref.make_background_mode(imgs)
+    assert got[0, 0] == 1 / 255.0 and got[0, 1] == 1 / 255.0
+    rng = np.random.default_rng(0)
+    st = rng.integers(0, 5, (11, 6, 7)).astype(np.uint8)
+    m = ref.make_background_mode(st)
+    for y in range(6):
+        for x in range(7):
+            assert m[y, x] == np.argmax(np.bincount(st[:, y, x], minlength=256)) / 255.0
+
+
+def test_pad_with_mean_placement():
+    """pad_with_mean (utils.jl:319-325) places a Julia (h, w) image at rows
+    div(p,2)-div(h,2)+1.. and columns div(p,2)-div(w,2)+1..; here (w, h) order."""
+    img = np.arange(15, dtype=np.float32).reshape(3, 5)        # Julia (h=5, w=3)
+    out = ref.pad_with_mean(img, 9)
+    assert out.shape == (9, 9)
+    o_fast, o_slow = 9 // 2 - 5 // 2, 9 // 2 - 3 // 2
+    assert np.array_equal(out[o_slow:o_slow + 3, o_fast:o_fast + 5], img)
+    assert np.all(out[0] == np.float32(7.0))
