@@ -200,6 +200,19 @@ PH_API int32_t ph_reconst_binary_vol(ph_ctx *ctx, uint8_t *vol, float threshold,
                                      const void *tf_front, const void *tf_dz, int32_t n_fast, int32_t n_slow,
                                      int32_t slices, void *stream);
 
+/* The sub-volumes particle_coordinates / particle_coor_diams cut out of the N0f8
+ * volume (particle_detection.jl:146-208), produced without the volume:
+ * boxes_host holds `count` records of 6 int64 in the reference's particle_bbs
+ * order (x_min, y_min, z_min, x_max, y_max, z_max), 1-based inclusive, x the
+ * slow axis (Julia column), y the fast axis (Julia row), z the slice.  Sub-volume
+ * i is d_vol[y_min:y_max, x_min:x_max, z_min:z_max] of cu_get_reconst_vol(...,
+ * N0f8) (holofunc.jl:184-200), stored [z][x][y] (fast y) at byte
+ * offsets_host[i] of `out`; offsets_host[count] = total bytes.  With out NULL
+ * only the offsets are written.  Only the slices any box covers are computed. */
+PH_API int32_t ph_reconst_subvolumes(ph_ctx *ctx, uint8_t *out, int64_t *offsets_host, const int64_t *boxes_host,
+                                     int32_t count, const void *wf, const void *tf_front, const void *tf_dz,
+                                     int32_t n_fast, int32_t n_slow, int32_t slices, void *stream);
+
 /* cu_get_reconst_vol_and_xyprojection_padded (holofunc.jl:339-364): wf is
  * n x n, the transfer functions 2n x 2n; vol is N0f8 n x n x slices (the centre
  * crop); return_dtype is the reference's `return_type` (N0F8/F16/F32/F64). */

@@ -10,7 +10,8 @@ The directory name is not a Python identifier; load the package with
 """
 from . import _lib
 from .batch import ReconBatch
-from .detection import cu_get_reconst_binary_vol, slice_bounding_boxes
+from .detection import (cu_get_reconst_binary_vol, cu_reconst_subvolumes, particle_coordinates,
+                        slice_bounding_boxes)
 from .serve import Server
 from .ccl import (count_labels, cu_bounding_rectangles, cu_connected_component_labeling,
                   cu_connected_component_labeling_batch, cu_find_valid_labels)

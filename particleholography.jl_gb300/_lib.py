@@ -60,6 +60,7 @@ SIGNATURES = {
     "ph_reconst_xyproj": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "ph_reconst_xyproj_lpf": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "ph_reconst_binary_vol": (_i32, [_vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
+    "ph_reconst_subvolumes": (_i32, [_vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "ph_reconst_vol": (_i32, [_vp, _vp, _i32, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "ph_reconst_vol_padded": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _vp]),
     "ph_propagate": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _vp]),

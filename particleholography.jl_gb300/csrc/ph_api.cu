@@ -671,12 +671,18 @@ ReconLayout recon_layout(ph_ctx *ctx, int nx, int ny, int ny_out, int nx_out, in
     return L;
 }
 
-enum ReconKind { RK_PROJ, RK_VOL, RK_CVOL, RK_PADDED };
+enum ReconKind { RK_PROJ, RK_VOL, RK_CVOL, RK_PADDED, RK_SUB };
+
+// Device tables of a sub-volume reconstruction (pass B's EPI_SUB epilogue).
+struct SubArgs {
+    const int *row_ptr, *row_box;
+    const SubBox *boxes;
+};
 
 int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype, int nx,
                        int ny, int nx_out, int ny_out, int x0, int y0, int slices, int batch, float4 *state, float2 *t,
                        unsigned long long *p64, const float2 *tw_x, const float2 *tw_y, bool want_proj,
-                       cudaStream_t s, float threshold = 0.0f);
+                       cudaStream_t s, float threshold = 0.0f, int first = 0, const SubArgs *sub = nullptr);
 
 // Shared driver of every reconstruction entry point.
 int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype,
@@ -730,12 +736,12 @@ int recon_group(int nbatch, int nx_rows_a) {
 int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype, int nx,
                        int ny, int nx_out, int ny_out, int x0, int y0, int slices, int batch, float4 *state, float2 *t,
                        unsigned long long *p64, const float2 *tw_x, const float2 *tw_y, bool want_proj,
-                       cudaStream_t s, float threshold) {
+                       cudaStream_t s, float threshold, int first, const SubArgs *sub) {
     ReconLayout L{};
     L.batch = batch;
     const int row_blocks_a = (nx + recon_a_rows(ny) - 1) / recon_a_rows(ny);
-    for (int k0 = 0; k0 < slices; k0 += L.batch) {
-        const int nb = std::min(L.batch, slices - k0);
+    for (int k0 = first; k0 < first + slices; k0 += L.batch) {
+        const int nb = std::min(L.batch, first + slices - k0);
         const int group = recon_group(nb, row_blocks_a);
         ReconA a{};
         a.state = state;
@@ -753,6 +759,13 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
             ReconB<EPI_PROJ> b{};
             b.t = t; b.tw = tw_x; b.proj64 = p64; b.rows = ny_out; b.nx_out = nx_out; b.x0 = 0;
             b.k0 = k0; b.nbatch = nb; b.group = group; b.vol_slice_stride = (long long)nx_out * ny_out;
+            b.err = static_cast<int *>(ctx->small);
+            PH_TRY(pass(ctx, s, "recon_b",[&] { return launch_recon_b(nx, b, s); }));
+        } else if (kind == RK_SUB) {
+            ReconB<EPI_SUB> b{};
+            b.t = t; b.tw = tw_x; b.vol = vol; b.rows = ny_out; b.nx_out = nx_out; b.x0 = 0;
+            b.k0 = k0; b.nbatch = nb; b.group = group;
+            b.row_ptr = sub->row_ptr; b.row_box = sub->row_box; b.boxes = sub->boxes;
             b.err = static_cast<int *>(ctx->small);
             PH_TRY(pass(ctx, s, "recon_b",[&] { return launch_recon_b(nx, b, s); }));
         } else if (kind == RK_CVOL) {
@@ -1696,6 +1709,83 @@ int32_t ph_reconst_vol(ph_ctx *ctx, void *vol, int32_t vol_dtype, float *proj, c
     PH_TRY(reconstruct(ctx, vol_dtype == PH_C64 ? RK_CVOL : RK_VOL, proj, nullptr, vol, vol_dtype,
                        static_cast<const float2 *>(wf), static_cast<const float2 *>(tf_front),
                        static_cast<const float2 *>(tf_dz), n_fast, n_slow, slices, s));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_reconst_subvolumes(ph_ctx *ctx, uint8_t *out, int64_t *offsets_host, const int64_t *boxes_host,
+                              int32_t count, const void *wf, const void *tf_front, const void *tf_dz, int32_t n_fast,
+                              int32_t n_slow, int32_t slices, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(offsets_host, "offsets");
+    if (count < 0 || (count > 0 && boxes_host == nullptr)) { set_err(ctx, "boxes must hold count >= 0 records"); return PH_ERR_INVALID; }
+    if (slices < 1) { set_err(ctx, "slices must be >= 1. Got %d.", slices); return PH_ERR_SIZE; }
+    PH_TRY(check_len(ctx, n_fast, n_slow));
+    std::vector<SubBox> bx((size_t)count);
+    int64_t off = 0;
+    int zlo = slices, zhi = -1;
+    for (int i = 0; i < count; ++i) {
+        const int64_t *v = boxes_host + 6 * (size_t)i;   // x_min y_min z_min x_max y_max z_max (x slow, y fast)
+        if (!(1 <= v[0] && v[0] <= v[3] && v[3] <= n_slow && 1 <= v[1] && v[1] <= v[4] && v[4] <= n_fast &&
+              1 <= v[2] && v[2] <= v[5] && v[5] <= slices)) {
+            set_err(ctx, "box %d (%lld, %lld, %lld, %lld, %lld, %lld) lies outside the (%d, %d, %d) volume", i,
+                    (long long)v[0], (long long)v[1], (long long)v[2], (long long)v[3], (long long)v[4],
+                    (long long)v[5], n_fast, n_slow, slices);
+            return PH_ERR_SIZE;
+        }
+        SubBox &b = bx[i];
+        b.fx0 = (int)v[1] - 1; b.fx1 = (int)v[4] - 1;
+        b.sy0 = (int)v[0] - 1; b.sy1 = (int)v[3] - 1;
+        b.z0 = (int)v[2] - 1; b.z1 = (int)v[5] - 1;
+        b.nxb = b.fx1 - b.fx0 + 1;
+        b.nyb = b.sy1 - b.sy0 + 1;
+        b.off = off;
+        offsets_host[i] = off;
+        off += (int64_t)b.nxb * b.nyb * (b.z1 - b.z0 + 1);
+        zlo = std::min(zlo, b.z0);
+        zhi = std::max(zhi, b.z1);
+    }
+    offsets_host[count] = off;
+    if (out == nullptr || count == 0) PH_LEAVE(ctx);
+    PH_NONNULL(wf, "wavefront");
+    PH_NONNULL(tf_front, "transfer_front");
+    PH_NONNULL(tf_dz, "transfer_dz");
+    // boxes of each slow row (CSR)
+    std::vector<int> row_ptr((size_t)n_slow + 1, 0), row_box;
+    for (const SubBox &b : bx)
+        for (int y = b.sy0; y <= b.sy1; ++y) ++row_ptr[y + 1];
+    for (int y = 0; y < n_slow; ++y) row_ptr[y + 1] += row_ptr[y];
+    row_box.resize((size_t)row_ptr[n_slow]);
+    {
+        std::vector<int> fill(row_ptr.begin(), row_ptr.end() - 1);
+        for (int i = 0; i < count; ++i)
+            for (int y = bx[i].sy0; y <= bx[i].sy1; ++y) row_box[fill[y]++] = i;
+    }
+    const int nz = zhi - zlo + 1;
+    const int nx = n_fast, ny = n_slow;
+    ReconLayout L = recon_layout(ctx, nx, ny, ny, nx, nz);
+    Arena a;
+    a.off = L.total;
+    const size_t o_rp = a.take<int>(row_ptr.size()), o_rb = a.take<int>(std::max<size_t>(row_box.size(), 1)),
+                 o_bx = a.take<SubBox>(bx.size());
+    PH_TRY(ensure_scratch(ctx, a.off, s));
+    PH_CUDA(cudaMemcpyAsync(at<int>(ctx, o_rp), row_ptr.data(), row_ptr.size() * sizeof(int), cudaMemcpyHostToDevice, s),
+            "cudaMemcpyAsync");
+    if (!row_box.empty())
+        PH_CUDA(cudaMemcpyAsync(at<int>(ctx, o_rb), row_box.data(), row_box.size() * sizeof(int),
+                                cudaMemcpyHostToDevice, s), "cudaMemcpyAsync");
+    PH_CUDA(cudaMemcpyAsync(at<SubBox>(ctx, o_bx), bx.data(), bx.size() * sizeof(SubBox), cudaMemcpyHostToDevice, s),
+            "cudaMemcpyAsync");
+    const float2 *tw_x = nullptr, *tw_y = nullptr;
+    PH_TRY(get_twiddles(ctx, nx, s, &tw_x));
+    PH_TRY(get_twiddles(ctx, ny, s, &tw_y));
+    float4 *state = at<float4>(ctx, L.state);
+    PH_TRY(issue_spectrum(ctx, static_cast<const float2 *>(wf), static_cast<const float2 *>(tf_front),
+                          static_cast<const float2 *>(tf_dz), nx, ny, false, nx, ny, at<float2>(ctx, L.a1), state, tw_x,
+                          tw_y, at<double>(ctx, L.acc), at<float2>(ctx, L.mean), s));
+    const SubArgs sub{at<int>(ctx, o_rp), at<int>(ctx, o_rb), at<SubBox>(ctx, o_bx)};
+    PH_TRY(issue_recon_slices(ctx, RK_SUB, nullptr, nullptr, out, PH_N0F8, nx, ny, nx, ny, 0, 0, nz, L.batch, state,
+                              at<float2>(ctx, L.t), at<unsigned long long>(ctx, L.p64), tw_x, tw_y, false, s, 0.0f,
+                              zlo, &sub));
     PH_LEAVE(ctx);
 }
 

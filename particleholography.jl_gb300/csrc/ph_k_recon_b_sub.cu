@@ -1,0 +1,11 @@
+// Reconstruction pass B with the EPI_SUB epilogue (sub-volumes around boxes).
+#include "ph_launch.cuh"
+
+namespace ph {
+
+cudaError_t launch_recon_b(int n, const ReconB<EPI_SUB> &b, cudaStream_t s) {
+    const int groups = (b.nbatch + b.group - 1) / b.group;
+    return launch_len<false>(n, b, b.rows, groups, s);
+}
+
+}  // namespace ph

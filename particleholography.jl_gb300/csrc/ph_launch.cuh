@@ -131,6 +131,7 @@ int recon_a_rows(int n);   // rows per pass A CTA for transform length n
 cudaError_t launch_recon_b(int n, const ReconB<EPI_PROJ> &b, cudaStream_t s);
 cudaError_t launch_recon_b(int n, const ReconB<EPI_VOL> &b, cudaStream_t s);
 cudaError_t launch_recon_b(int n, const ReconB<EPI_CVOL> &b, cudaStream_t s);
+cudaError_t launch_recon_b(int n, const ReconB<EPI_SUB> &b, cudaStream_t s);
 cudaError_t launch_gs_row(int n, const GsRow<ROW_MID> &b, cudaStream_t s);
 cudaError_t launch_gs_row(int n, const GsRow<ROW_FINAL> &b, cudaStream_t s);
 cudaError_t launch_gs_row(int n, const GsRow<ROW_INV> &b, cudaStream_t s);

@@ -344,7 +344,15 @@ struct ReconA : PassBase {
 enum Epilogue {
     EPI_PROJ = 0,      // running min / argmin -> packed atomicMin
     EPI_VOL = 1,       // clamp + convert -> vol (optionally the min of the stored values)
-    EPI_CVOL = 2       // complex slice -> vol
+    EPI_CVOL = 2,      // complex slice -> vol
+    EPI_SUB = 3        // N0f8 values inside given boxes -> their sub-volumes
+};
+
+// One sub-volume: fast range [fx0, fx1], slow range [sy0, sy1], slices
+// [z0, z1] (0-based, inclusive), stored [z][slow][fast] at byte offset off.
+struct SubBox {
+    int fx0, fx1, sy0, sy1, z0, z1, nxb, nyb;
+    long long off;
 };
 
 __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
@@ -369,6 +377,9 @@ struct ReconB : PassBase {
     int *err;                        // raised if a bulk-copy wait times out
     int vol_dtype;                   // PH_N0F8 .. PH_F64, or PH_BOOL: intensity <= threshold
     float threshold;
+    const int *row_ptr;              // EPI_SUB: boxes of row y are row_box[row_ptr[y] .. row_ptr[y + 1])
+    const int *row_box;
+    const SubBox *boxes;
     int rows;                        // rows of T per slice
     int nx_out, x0;                  // stored columns [x0, x0 + nx_out)
     int k0, nbatch, group;
@@ -426,6 +437,10 @@ struct ReconB : PassBase {
         for (int s = 0; s < E; ++s) { minv[s] = __int_as_float(0x7f800000); mink[s] = 0; }
         const bool track_min = (EPI == EPI_PROJ) || (EPI == EPI_VOL && proj64 != nullptr);
 
+        int sub_b = 0, sub_e = 0;   // EPI_SUB: this row's box list
+        if constexpr (EPI == EPI_SUB) {
+            if (valid) { sub_b = row_ptr[y]; sub_e = row_ptr[y + 1]; }
+        }
         for (int b = b0; b < b1; ++b) {
             const int k = k0 + b;
             const int buf = (b - b0) & 1;
@@ -449,6 +464,16 @@ struct ReconB : PassBase {
                     if constexpr (EPI == EPI_PROJ) {
                         const float i2 = fmaf(v.x, v.x, v.y * v.y);
                         if (i2 < minv[slot]) { minv[slot] = i2; mink[slot] = k; }
+                    } else if constexpr (EPI == EPI_SUB) {
+                        if (sub_b == sub_e) return;
+                        const float i2 = clamp01(fmaf(v.x, v.x, v.y * v.y));
+                        const uint8_t q = (uint8_t)__float2uint_rn(i2 * 255.0f);   // N0f8, as EPI_VOL
+                        for (int i = sub_b; i < sub_e; ++i) {
+                            const SubBox bx = boxes[row_box[i]];
+                            if (k >= bx.z0 && k <= bx.z1 && x >= bx.fx0 && x <= bx.fx1)
+                                reinterpret_cast<uint8_t *>(vol)[bx.off + ((long long)(k - bx.z0) * bx.nyb + (y - bx.sy0)) *
+                                                                               bx.nxb + (x - bx.fx0)] = q;
+                        }
                     } else {
                         const int xo = x - x0;
                         if (!valid || xo < 0 || xo >= nx_out) return;

@@ -47,3 +47,62 @@ def slice_bounding_boxes(bin_vol: torch.Tensor) -> list:
             b[:, 0] -= s * per
             out[int(s)] = b
     return out
+
+
+def cu_reconst_subvolumes(wavefront, transfer_front, transfer_dz, slices: int, boxes) -> list:
+    """The N0f8 sub-volumes particle_coordinates cuts out of ``cu_get_reconst_vol``
+    (particle_detection.jl:146-208), computed without the volume.  ``boxes``:
+    rows ``(x_min, y_min, z_min, x_max, y_max, z_max)`` (particle_bbs order,
+    1-based inclusive, x the slow axis, y the fast axis).  Returns one uint8
+    tensor per box, shape ``(z, x, y)`` (raw N0f8 levels)."""
+    import ctypes
+    wf, tf, td = _recon_args(wavefront, transfer_front, transfer_dz)
+    _check_same(wf, tf, td)
+    bx = np.ascontiguousarray(np.asarray(boxes, dtype=np.int64).reshape(-1, 6))
+    count = len(bx)
+    offs = np.zeros(count + 1, dtype=np.int64)
+    ctx, s = _ctx_stream(wf)
+    nx, ny = int(wf.shape[1]), int(wf.shape[0])
+    ctx.call("ph_reconst_subvolumes", None, offs.ctypes.data, bx.ctypes.data if count else None, count, None, None,
+             None, nx, ny, int(slices), s)
+    out = torch.empty(max(int(offs[-1]), 1), dtype=torch.uint8, device=wf.device)
+    if count:
+        ctx.call("ph_reconst_subvolumes", out.data_ptr(), offs.ctypes.data, bx.ctypes.data, count, wf.data_ptr(),
+                 tf.data_ptr(), td.data_ptr(), nx, ny, int(slices), s)
+    res = []
+    for i, (x0, y0, z0, x1, y1, z1) in enumerate(bx.tolist()):
+        shape = (z1 - z0 + 1, x1 - x0 + 1, y1 - y0 + 1)
+        res.append(out[int(offs[i]):int(offs[i + 1])].view(shape))
+    return res
+
+
+def _gaussian_kernel(sigma: float = 5.0) -> np.ndarray:
+    """ImageFiltering's Kernel.gaussian((sigma,)): 4 ceil(sigma) + 1 taps, sum 1."""
+    h = 2 * int(np.ceil(sigma))
+    x = np.arange(-h, h + 1, dtype=np.float64)
+    k = np.exp(-x * x / (2 * sigma * sigma))
+    return k / k.sum()
+
+
+def particle_coordinates(boxes, subvols, sigma: float = 5.0) -> np.ndarray:
+    """particle_coordinates (particle_detection.jl:146-160) on device sub-volumes:
+    per box, the Tamura depth profile (std / mean of each slice), smoothed with
+    the Gaussian kernel (replicated ends), its first maximum z, and the centre of
+    mass of that slice.  Returns rows (x, y, z) in the reference's 1-based
+    volume coordinates (float64 host arithmetic)."""
+    k = _gaussian_kernel(sigma)
+    h = len(k) // 2
+    out = []
+    for (x0, y0, z0, *_), sv in zip(np.asarray(boxes, dtype=np.int64).reshape(-1, 6).tolist(), subvols):
+        v = sv.cpu().numpy().astype(np.float64) / 255.0                     # (z, x, y)
+        prof = np.array([sl.std(ddof=1) / sl.mean() if sl.size > 1 and sl.mean() != 0 else 0.0 for sl in v])
+        padded = np.concatenate([np.full(h, prof[0]), prof, np.full(h, prof[-1])])
+        smooth = np.array([np.dot(padded[i:i + len(k)], k) for i in range(len(prof))])
+        z = int(np.argmax(smooth))
+        sl = v[z]                                                            # (x = column j, y = row i)
+        tot = sl.sum()
+        jj, ii = np.meshgrid(np.arange(1, sl.shape[0] + 1), np.arange(1, sl.shape[1] + 1), indexing="ij")
+        x = (jj * sl).sum() / tot
+        y = (ii * sl).sum() / tot
+        out.append((x + x0 - 1, y + y0 - 1, z + 1 + z0 - 1))
+    return np.array(out, dtype=np.float64).reshape(-1, 3)

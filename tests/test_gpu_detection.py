@@ -59,3 +59,30 @@ def test_slice_boxes_match_oracle(ph, cuda):
         assert np.array_equal(per[k][:, 0], valid)
         assert [tuple(b) for b in per[k][:, 1:].tolist()] == ref.bounding_rectangles(lab, valid)
     assert sum(len(b) for b in per) > 0
+
+
+def test_subvolumes_equal_volume_crops(ph, cuda):
+    """ph_reconst_subvolumes: every box equals the same crop of the N0f8 volume,
+    without the volume being formed (edge, overlapping and one-voxel boxes)."""
+    n, S = 128, 10
+    wf, hf, hdz, *_ = _case(cuda, n, seed=11)
+    W, F, D = ph.CuWavefront(wf), ph.CuTransfer(hf), ph.CuTransfer(hdz)
+    vol = to_np(ph.cu_get_reconst_vol(W, F, D, S, ph.N0f8))         # (z, slow, fast) raw levels
+    boxes = np.array([[1, 1, 1, 10, 12, 3],            # corner
+                      [5, 7, 2, 40, 30, 9],            # overlaps the next
+                      [20, 20, 4, 60, 70, 10],
+                      [128, 128, 10, 128, 128, 10],    # one voxel at the far corner
+                      [64, 1, 5, 64, 128, 5],          # one full fast line
+                      [1, 100, 1, 128, 101, 10]])      # full slow range
+    subs = ph.cu_reconst_subvolumes(W, F, D, S, boxes)
+    assert len(subs) == len(boxes)
+    for (x0, y0, z0, x1, y1, z1), sv in zip(boxes.tolist(), subs):
+        want = vol[z0 - 1:z1, x0 - 1:x1, y0 - 1:y1]
+        assert tuple(sv.shape) == want.shape
+        assert np.array_equal(to_np(sv), want.astype(np.uint8) if want.dtype != np.uint8 else want)
+    with pytest.raises(AssertionError):
+        ph.cu_reconst_subvolumes(W, F, D, S, [[0, 1, 1, 2, 2, 2]])   # outside the volume (1-based)
+    coords = ph.particle_coordinates(boxes[:3], subs[:3])
+    assert coords.shape == (3, 3)
+    for (x0, y0, z0, x1, y1, z1), (x, y, z) in zip(boxes[:3].tolist(), coords.tolist()):
+        assert x0 <= x <= x1 and y0 <= y <= y1 and z0 <= z <= z1
