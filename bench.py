@@ -116,53 +116,68 @@ def algorithmic_bytes(name: str, cfg: dict, launches: int, slices_per_frame: int
 # ---------------------------------------------------------------- clocks
 
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi samples (every 50 ms) of the SM clock and the throttle reasons;
+    only the samples taken between mark_start() and mark_end() count."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
         self.device = device
         self.proc = None
+        self.t0 = self.t1 = None
         self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"ph_clocks_{os.getpid()}.csv"
 
     def start(self):
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        deadline = time.time() + 5.0          # wait for the first sample before the timed region
+        while time.time() < deadline and self.path.stat().st_size == 0:
+            time.sleep(0.02)
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
 
     def stop(self) -> dict:
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.1)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
         self.fh.close()
-        sm, mx, reasons = [], [], set()
+        from datetime import datetime
+        rows = []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.path.read_text().splitlines():
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                mx.append(float(parts[2]))
+                ts = datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(parts[2]), float(parts[3]),
+                             {nm for nm, v in zip(names, parts[6:10]) if v.lower() == "active"}))
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
         self.path.unlink(missing_ok=True)
-        if not sm:
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
-        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        inside = [r for r in rows if self.t0 is not None and self.t1 is not None and self.t0 <= r[0] <= self.t1]
+        use = inside or [min(rows, key=lambda r: abs(r[0] - (self.t0 or r[0])))]
+        reasons = set().union(*(r[3] for r in use))
+        return {"sm_mhz": statistics.median(r[1] for r in use), "sm_max_mhz": max(r[2] for r in use),
+                "reasons": sorted(reasons), "samples": len(use), "interval_ms": 50}
 
 
 # ---------------------------------------------------------------- CPU (oracle) frame sample
@@ -281,7 +296,7 @@ def cpu_mvoxel_per_s(cfg, t_it, t_slice, t_ccl) -> float:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)   # ~0.8 s timed: enough 50 ms clock samples
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
@@ -370,12 +385,14 @@ def main():
     l0 = ctx.launches
     torch.cuda.synchronize()
     torch.cuda.cudart().cudaProfilerStart()      # ncu --profile-from-start off captures the timed steps only
+    clocks.mark_start()
     for i in range(args.steps):
         flush.zero_()                     # L2 flush, outside the step's events
         ev[i][0].record(stream)
         frame(h1, h2)
         ev[i][1].record(stream)
     torch.cuda.synchronize()
+    clocks.mark_end()
     torch.cuda.cudart().cudaProfilerStop()
     launches = ctx.launches - l0
     clk = clocks.stop()
@@ -555,12 +572,14 @@ def batch_main(args, cfg, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     l0 = ctx.launches
+    clocks.mark_start()
     for i in range(args.steps):
         flush.zero_()
         ev[i][0].record(stream)
         batch.run()
         ev[i][1].record(stream)
     torch.cuda.synchronize()
+    clocks.mark_end()
     launches = ctx.launches - l0
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -700,6 +719,7 @@ def serve_main(args, cfg, rank, world, local):
     l0 = ctx.launches
     clocks = ClockSampler(local)
     clocks.start()
+    clocks.mark_start()
     t0 = time.perf_counter()
     tk, vox = [], 0
     for i in range(nsat):
@@ -729,6 +749,7 @@ def serve_main(args, cfg, rank, world, local):
         rows.append({"load": load, "offered_req_s": round(rate, 2), "achieved_req_s": round(nreq / span, 2),
                      "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
                      "requests": nreq})
+    clocks.mark_end()
     clk = clocks.stop()
     srv.close()
     p99_09 = next(r["p99_ms"] for r in rows if r["load"] == 0.9)

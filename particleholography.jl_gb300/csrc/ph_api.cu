@@ -244,6 +244,11 @@ __global__ void k_background_mean(double *out, const uint8_t *__restrict__ image
     out[p] = acc / (double)count;
 }
 
+__global__ void k_sqrt_f32(float *out, const float *in, size_t n) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = sqrtf(in[i]);
+}
+
 __global__ void k_sum_f32(const float *in, size_t n, double *acc) {
     double sx = 0.0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -1159,9 +1164,11 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
     Arena a;
     const size_t oa = a.take<float2>(n), ob = a.take<float2>(n);
     const size_t oh = staged ? a.take<float2>(n) : 0, ohi = staged ? a.take<float2>(n) : 0;
+    const size_t oa1 = staged ? a.take<float>(n) : 0, oa2 = staged ? a.take<float>(n) : 0;
     PH_TRY(ensure_scratch(ctx, a.off, s));
     float2 *bufa = at<float2>(ctx, oa), *bufb = at<float2>(ctx, ob);
     float2 *ht = staged ? at<float2>(ctx, oh) : nullptr, *hti = staged ? at<float2>(ctx, ohi) : nullptr;
+    float *amp1 = staged ? at<float>(ctx, oa1) : nullptr, *amp2 = staged ? at<float>(ctx, oa2) : nullptr;
     int *err = static_cast<int *>(ctx->small);
     const float2 *tw_x = nullptr, *tw_y = nullptr;
     PH_TRY(get_twiddles(ctx, nx, s, &tw_x));
@@ -1176,7 +1183,10 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
         dim3 tb(32, 8), tg((nx + 31) / 32, (ny + 31) / 32);
         k_transfer_rows<<<tg, tb, 0, s>>>(ht, static_cast<const float2 *>(transfer), nx, ny, scale);
         k_transfer_rows<<<tg, tb, 0, s>>>(hti, static_cast<const float2 *>(invtransfer), nx, ny, scale);
-        PH_TRY(launched(ctx, cudaGetLastError(), "transfer rows", 2));
+        // the amplitudes sqrt(I1), sqrt(I2) once per call, as the row passes would form them
+        k_sqrt_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(amp1, holo1, n);
+        k_sqrt_f32<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(amp2, holo2, n);
+        PH_TRY(launched(ctx, cudaGetLastError(), "transfer rows and amplitudes", 4));
     }
 
     FwdRowsT<FWD_SQRT_REAL> f{};
@@ -1191,14 +1201,14 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
         c.src = bufa; c.ht = ht; c.dst = bufb; c.tw = tw_y; c.err = err; c.nx = nx;
         PH_TRY(pass(ctx, s, "gs_col",[&] { return launch_gs_col_t(ny, c, s); }));
         GsRowMidT r2{};
-        r2.src = bufb; r2.holo = holo2; r2.dst = bufa; r2.tw = tw_x; r2.err = err; r2.nrows = ny;
+        r2.src = bufb; r2.holo = amp2; r2.dst = bufa; r2.tw = tw_x; r2.err = err; r2.nrows = ny;
         r2.resid = (last && residual) ? acc : nullptr;
         PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return launch_gs_row_t(nx, r2, s); }));
         c.src = bufa; c.ht = hti; c.dst = bufb;
         PH_TRY(pass(ctx, s, "gs_col",[&] { return launch_gs_col_t(ny, c, s); }));
         if (!last) {
             GsRowMidT r1{};
-            r1.src = bufb; r1.holo = holo1; r1.dst = bufa; r1.tw = tw_x; r1.err = err; r1.nrows = ny;
+            r1.src = bufb; r1.holo = amp1; r1.dst = bufa; r1.tw = tw_x; r1.err = err; r1.nrows = ny;
             PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return launch_gs_row_t(nx, r1, s); }));
         } else {
             GsRow<ROW_FINAL> r1{};

@@ -535,8 +535,13 @@ enum RowMode {
 };
 
 __device__ __forceinline__ float2 amplitude_replace(float2 u, float s) {
-    if (u.x == 0.0f && u.y == 0.0f) return make_float2(s, 0.0f);   // angle(0) == 0
-    const float inv = rhypotf(u.x, u.y);
+    const float n2 = fmaf(u.x, u.x, u.y * u.y);
+    if (n2 == 0.0f) {
+        if (u.x == 0.0f && u.y == 0.0f) return make_float2(s, 0.0f);   // angle(0) == 0
+    }
+    // 1/|u| from the hardware reciprocal square root where |u|^2 is a normal,
+    // representable float; rhypotf (scaled) for the rest
+    const float inv = (n2 > 1e-36f && n2 < 1e36f) ? rsqrtf(n2) : rhypotf(u.x, u.y);
     return make_float2(u.x * inv * s, u.y * inv * s);
 }
 
@@ -654,7 +659,7 @@ constexpr int staged_stride() {
 // the dense rows at the exchange-row offsets, so the transform runs in place.
 struct GsRowMidT : PassBase {
     const float2 *src;       // [ny][nx]
-    const float *holo;       // [ny][nx]
+    const float *holo;       // [ny][nx] amplitudes sqrt(I), computed once per call
     float2 *dst;             // [nx][ny]
     const float2 *tw;
     double *resid;           // nullable: [0] += (|u| - s)^2, [1] += s^2
@@ -721,7 +726,7 @@ struct GsRowMidT : PassBase {
             const bool valid = y < nrows;
             fft_row<N, E, true, true>(xr, j, tw, [&](int, int x) -> float2 { return xr[x]; },
                                       [&](int, int x, float2 v) -> float2 {
-                                          const float s = sqrtf(hr[x]);
+                                          const float s = hr[x];
                                           if (resid != nullptr && valid) {
                                               const double a = sqrt((double)v.x * v.x + (double)v.y * v.y) - (double)s;
                                               acc0 += a * a;
