@@ -104,6 +104,14 @@ __device__ __forceinline__ float2 twiddle_fp64(int i, int n) {   // W_n^i rounde
     return make_float2((float)c, (float)s);
 }
 
+__global__ void k_phase_table(double2 *tab, int n) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double s, c;
+    sincospi(2.0 * (double)j / (double)n, &s, &c);
+    tab[j] = make_double2(c, s);
+}
+
 __global__ void k_twiddle(float2 *tw, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -639,6 +647,7 @@ int issue_spectrum(ph_ctx *ctx, const float2 *wf, const float2 *hf, const float2
     c.hf = hf;
     c.hdz = hdz;
     c.lpf = lpf;
+    c.ptab = ctx->phase_tab;
     c.state = state;
     c.tw = tw_y;
     c.nx = nx;
@@ -968,7 +977,14 @@ int32_t ph_create(int32_t device, size_t hbm_budget_bytes, ph_ctx **out) {
     DeviceGuard g(device);
     if (cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&ctx->small, 256) != cudaSuccess || cudaMemset(ctx->small, 0, 256) != cudaSuccess) {
+        cudaMalloc(&ctx->small, 256) != cudaSuccess || cudaMemset(ctx->small, 0, 256) != cudaSuccess ||
+        cudaMalloc(&ctx->phase_tab, sizeof(double2) * kPhaseTable) != cudaSuccess) {
+        cudaGetLastError();
+        ph_destroy(ctx);
+        return PH_ERR_CUDA;
+    }
+    k_phase_table<<<(kPhaseTable + 255) / 256, 256>>>(ctx->phase_tab, kPhaseTable);
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
         cudaGetLastError();
         ph_destroy(ctx);
         return PH_ERR_CUDA;
@@ -991,6 +1007,7 @@ void ph_destroy(ph_ctx *ctx) {
         for (auto &kv : ctx->tw) cudaFree(kv.second);
         if (ctx->scratch) cudaFree(ctx->scratch);
         if (ctx->small) cudaFree(ctx->small);
+        if (ctx->phase_tab) cudaFree(ctx->phase_tab);
         if (ctx->done) cudaEventDestroy(ctx->done);
         if (ctx->capture_stream) cudaStreamDestroy(ctx->capture_stream);
         cudaGetLastError();

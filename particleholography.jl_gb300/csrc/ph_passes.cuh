@@ -164,11 +164,29 @@ struct FwdRowsT : PassBase {
 
 // ---------------------------------------------------------------- spectrum state
 
-// Phase of h as a 32-bit fixed-point fraction of a turn (FP64 atan2).
-__device__ __forceinline__ uint32_t phase_turns_u32(float2 h) {
-    const double a = atan2((double)h.y, (double)h.x) * 0.15915494309189533577;   // / 2 pi
-    const long long q = __double2ll_rn(a * 4294967296.0);
-    return (uint32_t)(unsigned long long)q;
+// Phase of h as a 32-bit fixed-point fraction of a turn, to ~1e-10 rad with
+// FP64 only where FP32 would lose it: the nearest of 4096 table angles j / 4096
+// turns (FP32 atan2 picks it), the rotation h * conj(w_j) in FP64 (tab holds
+// w_j = (cos, sin)(2 pi j / 4096), FP64), and the remaining angle |phi| <~
+// pi / 4096 by FP32 atan2, whose ~2 ulp relative error is then ~2e-10 rad.
+// (FP64 atan2 throughout costs ~7x more FP64 operations, which GB300 runs at
+// 1/64 of its FP32 rate.)
+constexpr int kPhaseTable = 4096;
+__device__ __forceinline__ uint32_t phase_turns_u32(float2 h, const double2 *__restrict__ tab) {
+    const float a0 = atan2f(h.y, h.x);
+    const int i = __float2int_rn(a0 * ((float)kPhaseTable / 6.28318530717958647692f));
+    const double2 w = __ldg(tab + (i & (kPhaseTable - 1)));
+    const double zx = (double)h.x * w.x + (double)h.y * w.y;   // h * conj(w)
+    const double zy = (double)h.y * w.x - (double)h.x * w.y;
+    const float phi = atan2f((float)zy, (float)zx);
+    return ((uint32_t)i << 20) + (uint32_t)__float2int_rn(phi * (4294967296.0f / 6.28318530717958647692f));
+}
+
+// |h| - 1: (|h|^2 - 1) in FP64 from exact products (no cancellation error
+// near |h| = 1), over |h| + 1 in FP32.
+__device__ __forceinline__ float modulus_minus_one(float2 h) {
+    const double v = (double)h.x * h.x + (double)h.y * h.y - 1.0;
+    return (float)v / (sqrtf(fmaf(h.x, h.x, h.y * h.y)) + 1.0f);
 }
 
 // Rows kx of the forward-row output, FFT along y, times the front transfer
@@ -178,6 +196,7 @@ struct SpectrumCols : PassBase {
     const float2 *a1;        // [nx][ny]
     const float2 *hf, *hdz;  // centred [ny][nx]
     const float *lpf;        // centred [ny][nx] low-pass filter, or null
+    const double2 *ptab;     // kPhaseTable unit vectors (phase_turns_u32)
     float4 *state;           // [nx][ny]
     const float2 *tw;
     int nx, ny;
@@ -197,8 +216,8 @@ struct SpectrumCols : PassBase {
                 const size_t c = (size_t)shift_idx(ky, N) * nx + sx;
                 const float2 x0 = cscale(cmul(v, hf[c]), lpf != nullptr ? scale * lpf[c] : scale);
                 const float2 d = hdz[c];
-                const float mag_m1 = (float)(sqrt((double)d.x * d.x + (double)d.y * d.y) - 1.0);
-                state[(size_t)kx * N + ky] = make_float4(x0.x, x0.y, __uint_as_float(phase_turns_u32(d)), mag_m1);
+                state[(size_t)kx * N + ky] =
+                    make_float4(x0.x, x0.y, __uint_as_float(phase_turns_u32(d, ptab)), modulus_minus_one(d));
             });
     }
 };
