@@ -77,6 +77,17 @@ struct FftPlan {
     __host__ __device__ static constexpr int tw_offset() { return plan_tw_offset(N, E, S); }
 };
 
+// Input q-th consumed by dft<R>: the split radices (R = P x Q, see dft_split)
+// read inputs Q*n1 + n2 with n2 outer and n1 inner.
+template <int R>
+__host__ __device__ constexpr int dft_input_order(int q) {
+    return R == 16 ? 4 * (q % 4) + q / 4
+         : R == 8  ? 4 * (q % 2) + q / 2
+         : R == 32 ? 8 * (q % 4) + q / 4
+         : R == 64 ? 8 * (q % 8) + q / 8
+                   : q;
+}
+
 // Shared-memory index of column i of a row: one pad element per 16 keeps the
 // strided stage writes free of bank conflicts.
 __device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
@@ -160,12 +171,13 @@ __device__ __forceinline__ void fft_row_sync(float2 *__restrict__ srow, int j, c
             constexpr bool FIRST = (S == 0);
             constexpr bool LASTSTAGE = (S == PL::NSTAGES - 1);
 
-            // ---- gather inputs
+            // ---- gather inputs, in the order the butterfly consumes them
 #pragma unroll
             for (int m = 0; m < M; ++m) {
                 const int b = j + m * P;
 #pragma unroll
-                for (int r = 0; r < R; ++r) {
+                for (int q = 0; q < R; ++q) {
+                    const int r = dft_input_order<R>(q);
                     const int col = b + r * STRIDE_IN;
                     if constexpr (FIRST) {
                         v[m * R + r] = load(m * R + r, col);
@@ -185,7 +197,10 @@ __device__ __forceinline__ void fft_row_sync(float2 *__restrict__ srow, int j, c
                     const int k = b & (NS - 1);
                     constexpr int TOFF = PL::template tw_offset<S>();
 #pragma unroll
-                    for (int r = 1; r < R; ++r) t[r] = cmul(t[r], load_tw<INV>(tw, TOFF + (r - 1) * NS + k));
+                    for (int q = 0; q < R; ++q) {
+                        const int r = dft_input_order<R>(q);
+                        if (r > 0) t[r] = cmul(t[r], load_tw<INV>(tw, TOFF + (r - 1) * NS + k));
+                    }
                 }
                 dft<R, INV>(t);
 #pragma unroll
