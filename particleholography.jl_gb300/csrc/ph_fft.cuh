@@ -112,6 +112,31 @@ __device__ __forceinline__ float2 load_tw(const float2 *__restrict__ tw, int i) 
     return w;
 }
 
+// The stage blocks of the table (entries [B, size), B = N: all that the stages
+// read) copied to shared memory; p[0] holds entry B.
+template <int B>
+struct SmemTw {
+    const float2 *p;
+};
+template <bool INV, int B>
+__device__ __forceinline__ float2 load_tw(const SmemTw<B> &tw, int i) {
+    float2 w = tw.p[i - B];
+    if (INV) w.y = -w.y;
+    return w;
+}
+template <int N, int E>
+constexpr size_t stage_tw_bytes() {
+    return ((size_t)(plan_tw_size(N, E) - plan_tw_offset(N, E, 1)) * 8 + 127) / 128 * 128;
+}
+// Every thread of the CTA calls this; the copy is visible after the next CTA barrier.
+template <int N, int E>
+__device__ __forceinline__ SmemTw<N> stage_tw_to_smem(float2 *dst, const float2 *__restrict__ tw) {
+    constexpr int B = plan_tw_offset(N, E, 1);
+    constexpr int C = plan_tw_size(N, E) - B;
+    for (int i = threadIdx.x; i < C; i += blockDim.x) dst[i] = __ldg(tw + B + i);
+    return SmemTw<N>{dst};
+}
+
 // Value the OUT_SMEM variant writes to shared memory: the store callback's result.
 template <bool OUT_SMEM, class Store>
 __device__ __forceinline__ float2 smem_out_value(Store &store, int slot, int col, float2 v) {
@@ -138,14 +163,15 @@ struct RowSync {
 // Runs one length-N transform per row.  Every thread that `sync` covers must
 // call it.  `srow` is this thread's shared row.
 //
+//   tw:    the twiddle table (global pointer) or its stage blocks in shared memory (SmemTw)
 //   Load:  float2 load(int slot, int col)   -- slot = m*R0 + r (compile-time after unrolling)
 //   Store: void store(int slot, int col, float2 v)
 //   OUT_SMEM: write the outputs to srow (after an internal barrier) and call
 //             store() first so it may transform the value; ends with a barrier.
 //             store() must then RETURN the value to write: float2 store(slot, col, v).
-template <int N, int E, bool INV, bool OUT_SMEM = false, class Load, class Store, class Sync>
-__device__ __forceinline__ void fft_row_sync(float2 *__restrict__ srow, int j, const float2 *__restrict__ tw,
-                                             Load &&load, Store &&store, const Sync &sync) {
+template <int N, int E, bool INV, bool OUT_SMEM = false, class Tw, class Load, class Store, class Sync>
+__device__ __forceinline__ void fft_row_sync(float2 *__restrict__ srow, int j, const Tw tw, Load &&load,
+                                             Store &&store, const Sync &sync) {
     using PL = FftPlan<N, E>;
     constexpr int P = PL::P;
     float2 v[E];
@@ -237,9 +263,8 @@ __device__ __forceinline__ void fft_row_sync(float2 *__restrict__ srow, int j, c
 }
 
 // The transform with CTA-wide barriers.
-template <int N, int E, bool INV, bool OUT_SMEM = false, class Load, class Store>
-__device__ __forceinline__ void fft_row(float2 *__restrict__ srow, int j, const float2 *__restrict__ tw,
-                                        Load &&load, Store &&store) {
+template <int N, int E, bool INV, bool OUT_SMEM = false, class Tw, class Load, class Store>
+__device__ __forceinline__ void fft_row(float2 *__restrict__ srow, int j, const Tw tw, Load &&load, Store &&store) {
     fft_row_sync<N, E, INV, OUT_SMEM>(srow, j, tw, load, store, CtaSync{});
 }
 

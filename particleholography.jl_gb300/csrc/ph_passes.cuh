@@ -11,10 +11,11 @@
 //   spectrum state            [nx][ny]   float4 (re, im, phase-rate bits, |Hdz|-1)
 //   slice intermediate T      [batch][ny][nx]
 //
-// The reconstruction passes stage their input rows in shared memory with bulk
-// asynchronous copies (TMA, ph_tma.cuh): pass A loads its spectrum-state rows
-// once and transforms several slices from them; pass B double-buffers the rows
-// of the next slice while it transforms the current one.
+// The reconstruction passes stage their input rows in shared memory: pass A
+// forms X at its first slice and Hdz from the spectrum-state rows once and
+// advances X slice by slice; pass B double-buffers the rows of the next slice
+// with bulk asynchronous copies (TMA, ph_tma.cuh) while it transforms the
+// current one.
 //
 // Each pass chooses its elements per thread (EPT, the main radix), its CTA size
 // (TT) and the resident threads per SM its register budget is sized for (RTS):
@@ -30,6 +31,9 @@
 #endif
 #ifndef PH_RECONB_RTS
 #define PH_RECONB_RTS 640
+#endif
+#ifndef PH_RECONA_CHAIN
+#define PH_RECONA_CHAIN -1   // pass A product chain: -1 per length (chain<N>()), 0 never, 1 always
 #endif
 
 namespace ph {
@@ -83,6 +87,18 @@ struct PassBase {
 };
 
 constexpr size_t round128(size_t b) { return (b + 127) / 128 * 128; }
+
+// Whether the stage twiddles of a length-N, E-per-thread transform also fit in
+// the shared memory of a pass that uses `used` bytes (the copy starts at
+// round128(used)), and the bytes they add.
+template <int N, int E>
+constexpr bool tw_fits(size_t used) {
+    return round128(used) + stage_tw_bytes<N, E>() <= kSmemMax;
+}
+template <int N, int E>
+constexpr size_t tw_extra(size_t used) {
+    return tw_fits<N, E>(used) ? round128(used) - used + stage_tw_bytes<N, E>() : 0;
+}
 
 // The pointer, hidden from the optimiser: loads through it are not hoisted
 // out of the enclosing loop (which would pin the values in registers).
@@ -224,14 +240,15 @@ struct SpectrumCols : PassBase {
 
 // ---------------------------------------------------------------- reconstruction pass A
 
-// Slice k of rows kx: X_k = X0 * Hdz^k evaluated directly from the phase rate
-// (exact integer turn arithmetic) and |Hdz|^k ~ 1 + k (|Hdz| - 1); inverse FFT
-// along ky; transposed store T[b][y - y0][kx] for y in [y0, y0 + ny_out).
+// Slice k of rows kx: X_k = X0 * Hdz^k; inverse FFT along ky; transposed store
+// T[b][y - y0][kx] for y in [y0, y0 + ny_out).  Hdz^k X0 evaluated directly
+// from the state uses the phase rate times k in exact integer turn arithmetic
+// and |Hdz|^k ~ 1 + k (|Hdz| - 1).
 //
-// A CTA loads the spectrum-state rows of its ROWS rows into shared memory once
-// (one bulk copy per row) and transforms `group` consecutive slices from them.
-// The state rows are spaced so that the 16-byte loads of a phase of 8 lanes
-// (ROWS rows x 8/ROWS columns) fall on distinct banks.
+// A CTA transforms `group` consecutive slices from rows staged in shared
+// memory once (the two forms are described at `chain`).  Staged rows are
+// spaced so that the accesses of one phase of lanes (ROWS rows x consecutive
+// columns) fall on distinct banks.
 //
 // The transposed store writes 4 consecutive kx (one 32-byte sector) per y.
 // Where a CTA holds fewer than 4 rows (N >= 4096), 4 / ROWS CTAs form a
@@ -255,34 +272,68 @@ struct ReconA : PassBase {
     int k0;                // global slice index of batch slot 0
     int nbatch, group;     // slices in the batch, slices per CTA
 
+    // Two staged forms.
+    //  chain: shared memory holds, per row, X_k and Hdz as two float2 rows;
+    //    every slice reads X_k and advances it in place, X_{k+1} = X_k Hdz (the
+    //    reference's cumulative product).  The CTA computes X at its first
+    //    slice directly from the state, so each product chain spans at most
+    //    `group` slices.
+    //  direct: the state rows are staged by bulk copy and every slice
+    //    evaluates Hdz^k from them.
+    // The chain saves the per-voxel sin/cos; the direct form moves fewer
+    // shared-memory bytes per voxel and needs fewer registers.  Measured per
+    // pass A launch, chain against direct: 2048 3.7 % faster; 1024 18 % slower
+    // (register spills); 4096 2.7 % slower (its cluster store competes for
+    // shared-memory bandwidth).  Other lengths keep the direct form.
+    template <int N>
+    static constexpr bool chain() {
+        return PH_RECONA_CHAIN >= 0 ? PH_RECONA_CHAIN != 0 : N == 2048;
+    }
+    template <int N, bool RF>
+    static constexpr int rec_stride() {   // float2 between rows: conflict-free for the load pattern
+        using S = Shape<N, EPT, TT>;
+        return N + SmemRow<N, S::ROWS, S::P, RF>::JC % 16;
+    }
     template <int N>
     static constexpr size_t state_stride() {   // bytes between staged state rows
         constexpr int R = Shape<N, EPT, TT>::ROWS;
         constexpr size_t dense = (size_t)N * 16;
         return (dense + 127) / 128 * 128 + (16 * (8 / (R < 8 ? R : 8))) % 128;
     }
-    // Staged when the state rows and the exchange rows fit the CTA's shared memory.
+    template <int N, bool RF>
+    static constexpr size_t stage_bytes() {   // staged rows (+ the bulk-copy barrier of the direct form)
+        return chain<N>() ? round128((size_t)2 * Shape<N, EPT, TT>::ROWS * rec_stride<N, RF>() * 8)
+                          : round128((size_t)Shape<N, EPT, TT>::ROWS * state_stride<N>() + 8);
+    }
+    // Staged when the staged rows and the exchange rows fit the CTA's shared memory.
     template <int N, bool RF>
     static constexpr bool staged() {
-        return (size_t)Shape<N, EPT, TT>::ROWS * state_stride<N>() + Shape<N, EPT, TT>::template smem_bytes<RF>() +
-                   16 <= kSmemMax;
+        return stage_bytes<N, RF>() + Shape<N, EPT, TT>::template smem_bytes<RF>() <= kSmemMax;
     }
     template <int N, bool RF>
     static constexpr size_t stage_total() {
-        return staged<N, RF>() ? (size_t)Shape<N, EPT, TT>::ROWS * state_stride<N>() : 0;
+        return staged<N, RF>() ? stage_bytes<N, RF>() : 0;
     }
     template <int N, bool RF>
     static constexpr size_t smem() {
-        return stage_total<N, RF>() + Shape<N, EPT, TT>::template smem_bytes<RF>() + 16;
+        return stage_total<N, RF>() + Shape<N, EPT, TT>::template smem_bytes<RF>();
+    }
+    // Hdz^k X0 from the state (re, im, phase-rate bits, |Hdz| - 1).
+    __device__ __forceinline__ static float2 direct(const float4 s, uint32_t k) {
+        const int32_t tt = (int32_t)(k * __float_as_uint(s.z));
+        const float ang = (float)tt * 1.46291807926715968e-9f;   // 2 pi / 2^32
+        float sn, cs;
+        __sincosf(ang, &sn, &cs);
+        const float mag = fmaf((float)k, s.w, 1.0f);
+        return cmul(make_float2(s.x, s.y), make_float2(cs * mag, sn * mag));
     }
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
         using S = Shape<N, EPT, TT>;
         constexpr int ROWS = S::ROWS;
-        constexpr size_t SS = state_stride<N>();
+        constexpr bool CHAIN = staged<N, RF>() && chain<N>();
         unsigned char *xbase = smem + stage_total<N, RF>();
-        uint64_t *bar = reinterpret_cast<uint64_t *>(xbase + S::template smem_bytes<RF>());
         constexpr int CS = cluster<N>();
         // The CTAs of one row block (its `gridDim.y` slice groups) are consecutive
         // in launch order, so they run together and share its state rows in L2.
@@ -291,16 +342,41 @@ struct ReconA : PassBase {
         const int g = CS == 1 ? lin % gridDim.y : blockIdx.y;
         const int kx0 = (CS == 1 ? lin / gridDim.y : blockIdx.x) * ROWS;
         const int kx = kx0 + r;
-        const bool valid = kx < nx;
-        const float4 *srow;
-        if constexpr (staged<N, RF>()) {
+        const bool valid = kx < nx;   // (CTAs that only pad a cluster hold no valid row)
+        const int b0 = g * group;
+        const int b1 = min(b0 + group, nbatch);
+        const float4 *srow = state + (size_t)(valid ? kx : 0) * N;
+        float2 *xs = nullptr, *hs = nullptr;
+        if constexpr (CHAIN) {
+            constexpr int XS = rec_stride<N, RF>();
+            xs = reinterpret_cast<float2 *>(smem) + (size_t)r * XS;
+            hs = reinterpret_cast<float2 *>(smem) + (size_t)(ROWS + r) * XS;
+            const uint32_t kf = (uint32_t)(k0 + b0);
+#pragma unroll
+            for (int q = 0; q < S::E; ++q) {
+                const int col = in_col<N, S::E>(j, q);   // the columns this thread's first stage reads
+                float2 x = make_float2(0.0f, 0.0f), h = x;
+                if (valid) {
+                    const float4 st = srow[col];
+                    x = direct(st, kf);
+                    // Hdz itself: the accurate sin/cos, as its error grows along the chain
+                    float sn, cs;
+                    sincospif((float)(int32_t)__float_as_uint(st.z) * 4.656612873077392578125e-10f, &sn, &cs);
+                    const float mag = 1.0f + st.w;
+                    h = make_float2(cs * mag, sn * mag);
+                }
+                xs[col] = x;
+                hs[col] = h;
+            }
+        } else if constexpr (staged<N, RF>()) {
+            constexpr size_t SS = state_stride<N>();
+            uint64_t *bar = reinterpret_cast<uint64_t *>(smem + ROWS * SS);
             if (threadIdx.x == 0) {
                 mbar_init(bar, 1);
                 mbar_fence_init();
             }
             __syncthreads();
             if (threadIdx.x == 0) {
-                // (CTAs that only pad a cluster hold no valid row)
                 const int nvalid = max(0, min(ROWS, nx - kx0));
                 mbar_arrive_expect_tx(bar, (uint32_t)(nvalid * N * 16));
                 for (int q = 0; q < nvalid; ++q)
@@ -308,25 +384,19 @@ struct ReconA : PassBase {
             }
             mbar_wait(bar, 0, err);
             srow = reinterpret_cast<const float4 *>(smem + (size_t)r * SS);
-        } else {
-            srow = state + (size_t)(valid ? kx : 0) * N;
         }
         float2 *xr = xrow<N, EPT, TT, RF>(xbase, r);
-        const int b0 = g * group;
-        const int b1 = min(b0 + group, nbatch);
         for (int b = b0; b < b1; ++b) {
             const uint32_t k = (uint32_t)(k0 + b);
-            const float kf = (float)k;
             float2 *tb = t + (size_t)b * ny_out * nx;
             auto load = [&](int, int ky) -> float2 {
-                const float4 s = srow[ky];
-                const int32_t tt = (int32_t)(k * __float_as_uint(s.z));
-                const float ang = (float)tt * 1.46291807926715968e-9f;   // 2 pi / 2^32
-                float sn, cs;
-                __sincosf(ang, &sn, &cs);
-                const float mag = fmaf(kf, s.w, 1.0f);
-                const float2 g = make_float2(cs * mag, sn * mag);
-                return cmul(make_float2(s.x, s.y), g);
+                if constexpr (CHAIN) {
+                    const float2 x = xs[ky];   // written by this thread only
+                    xs[ky] = cmul(x, hs[ky]);
+                    return x;
+                } else {
+                    return direct(srow[ky], k);
+                }
             };
             if constexpr (CS == 1) {
                 fft_row<N, S::E, true>(xr, j, tw, load, [&](int, int y, float2 v) {
@@ -799,7 +869,9 @@ struct GsColT : PassBase {
     template <int N>
     static constexpr bool persistent() { return true; }
     template <int N, bool RF>
-    static constexpr size_t smem() { return 2 * fbytes<N>() + hbytes<N>() + 32; }
+    static constexpr size_t smem() {
+        return 2 * fbytes<N>() + hbytes<N>() + 32 + tw_extra<N, S<N>::E>(2 * fbytes<N>() + hbytes<N>() + 32);
+    }
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
@@ -811,6 +883,13 @@ struct GsColT : PassBase {
         constexpr size_t FB = fbytes<N>(), HB = hbytes<N>();
         unsigned char *hbase = smem + 2 * FB;
         uint64_t *bars = reinterpret_cast<uint64_t *>(hbase + HB);   // [0], [1] field buffers, [2] transfer
+        // The stage twiddles in shared memory where they fit: 4.7 % faster at
+        // 2048 than reading them through L1 (the row pass and pass A measured
+        // slower with the same copy, so they read the table in global memory).
+        constexpr size_t U = 2 * FB + HB + 32;
+        constexpr bool TWS = tw_fits<N, E>(U);
+        SmemTw<N> tws{nullptr};
+        if constexpr (TWS) tws = stage_tw_to_smem<N, E>(reinterpret_cast<float2 *>(smem + round128(U)), tw);
         const int nblocks = (nx + ROWS - 1) / ROWS;
         auto issue_field = [&](int rb, int buf) {
             const int kb = rb * ROWS, nv = min(ROWS, nx - kb);
@@ -854,15 +933,18 @@ struct GsColT : PassBase {
             const float2 *hr = reinterpret_cast<const float2 *>(hbase) + (size_t)r * HS;
             const int kx = rb * ROWS + r;
             const bool valid = kx < nx;
-            const float2 *tw = opaque(this->tw);   // twiddles are re-read per block, not held in registers
-            fft_row<N, E, false, true>(xr, j, tw, [&](int, int y) -> float2 { return xr[y]; },
-                                       [&](int, int ky, float2 v) -> float2 { return cmul(v, hr[ky]); });
-            // the transform ended with a barrier: the transfer rows are free
-            if (HT_EARLY && threadIdx.x == 0 && next < nblocks) issue_ht(next);
-            fft_row<N, E, true>(xr, j, tw, [&](int, int ky) -> float2 { return xr[spad(ky)]; },
-                                [&](int, int y, float2 v) {
-                                    if (valid) dst[(size_t)y * nx + kx] = v;
-                                });
+            auto go = [&](const auto twv) {
+                fft_row<N, E, false, true>(xr, j, twv, [&](int, int y) -> float2 { return xr[y]; },
+                                           [&](int, int ky, float2 v) -> float2 { return cmul(v, hr[ky]); });
+                // the transform ended with a barrier: the transfer rows are free
+                if (HT_EARLY && threadIdx.x == 0 && next < nblocks) issue_ht(next);
+                fft_row<N, E, true>(xr, j, twv, [&](int, int ky) -> float2 { return xr[spad(ky)]; },
+                                    [&](int, int y, float2 v) {
+                                        if (valid) dst[(size_t)y * nx + kx] = v;
+                                    });
+            };
+            if constexpr (TWS) go(tws);
+            else go(opaque(this->tw));   // twiddles are re-read per block, not held in registers
         }
     }
 };

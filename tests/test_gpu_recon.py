@@ -137,7 +137,8 @@ def test_graph_replay_matches_direct_launches(ph, cuda):
 
 
 def test_slice_batches_agree(ph, cuda):
-    """The result does not depend on how slices are batched between the passes."""
+    """The result does not depend on how slices are batched between the passes
+    (at this size every slice group holds one slice: bit for bit)."""
     from ph_gb300 import _lib
     holo, hf, hdz = _case(128, seed=9)
     wf = ph.cu_gabor_wavefront(to_dev(holo, cuda))
@@ -150,3 +151,27 @@ def test_slice_batches_agree(ph, cuda):
     ctx.set_option(_lib.PH_OPT_SLICE_BATCH, 0)
     for p, a in outs[1:]:
         assert np.array_equal(p, outs[0][0]) and np.array_equal(a, outs[0][1])
+
+
+def test_long_slice_groups(ph, cuda):
+    """Slice groups of many slices, where pass A advances X by the Hdz product
+    chain within each group, against the oracle's chain from slice 0; batchings
+    that split the groups differently agree to rounding."""
+    from ph_gb300 import _lib
+    n, slices = 1024, 96
+    holo, hf, hdz = _case(n, seed=11, z0=-2000.0, dz=-100.0)
+    p_ref, a_ref = ref.reconst_xyprojection(ref.gabor_wavefront(holo), hf, hdz, slices, with_argmin=True)
+    wf = ph.cu_gabor_wavefront(to_dev(holo, cuda))
+    args = (wf, ph.CuTransfer(to_dev(hf, cuda)), ph.CuTransfer(to_dev(hdz, cuda)), slices)
+    ctx = _lib.default_context(0)
+    outs = []
+    try:
+        for b in (0, 16, 40):
+            ctx.set_option(_lib.PH_OPT_SLICE_BATCH, b)
+            outs.append([to_np(t) for t in ph.cu_get_reconst_xyprojection(*args, return_argmin=True)])
+    finally:
+        ctx.set_option(_lib.PH_OPT_SLICE_BATCH, 0)
+    for p, a in outs:
+        assert rel_l2(p, p_ref) < REL_L2
+        assert np.mean(a == a_ref) >= ARGMIN_AGREE
+        assert rel_l2(p, outs[0][0]) < 1e-5
