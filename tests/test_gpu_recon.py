@@ -154,11 +154,11 @@ def test_slice_batches_agree(ph, cuda):
 
 
 def test_long_slice_groups(ph, cuda):
-    """Slice groups of many slices, where pass A advances X by the Hdz product
-    chain within each group, against the oracle's chain from slice 0; batchings
-    that split the groups differently agree to rounding."""
+    """Slice groups of many slices at length 2048, where pass A advances X by
+    the Hdz product chain within each group, against the oracle's chain from
+    slice 0; batchings that split the groups differently agree to rounding."""
     from ph_gb300 import _lib
-    n, slices = 1024, 96
+    n, slices = 2048, 64
     holo, hf, hdz = _case(n, seed=11, z0=-2000.0, dz=-100.0)
     p_ref, a_ref = ref.reconst_xyprojection(ref.gabor_wavefront(holo), hf, hdz, slices, with_argmin=True)
     wf = ph.cu_gabor_wavefront(to_dev(holo, cuda))
