@@ -386,6 +386,7 @@ struct ReconA : PassBase {
             srow = reinterpret_cast<const float4 *>(smem + (size_t)r * SS);
         }
         float2 *xr = xrow<N, EPT, TT, RF>(xbase, r);
+        if constexpr (CS > 1) cluster_arrive();   // pairs with the first slice's wait
         for (int b = b0; b < b1; ++b) {
             const uint32_t k = (uint32_t)(k0 + b);
             float2 *tb = t + (size_t)b * ny_out * nx;
@@ -405,7 +406,19 @@ struct ReconA : PassBase {
                     if (valid && yo >= 0 && yo < ny_out) __stcs(tb + (size_t)yo * nx + kx, v);
                 });
             } else {
-                fft_row<N, S::E, true, true>(xr, j, tw, load, [](int, int, float2 v) -> float2 { return v; });
+                // The first barrier of the transform (before its first exchange
+                // write) waits for the cluster: the peers have read this CTA's
+                // rows of the previous slice.  The last one (after the output
+                // write) is the cluster barrier that follows.
+                constexpr int LAST_SYNC = 2 * FftPlan<N, S::E>::NSTAGES - 1;
+                int nsync = 0;
+                const auto sync = [&nsync]() {
+                    const int i = nsync++;
+                    if (i == 0) cluster_wait();
+                    else if (i != LAST_SYNC) __syncthreads();
+                };
+                fft_row_sync<N, S::E, true, true>(xr, j, tw, load, [](int, int, float2 v) -> float2 { return v; },
+                                                  sync);
                 cluster_sync();   // every CTA of the cluster holds its transformed rows
                 constexpr int RS = S::template stride<RF>();
                 constexpr int YS = N / CS;   // y range each CTA stores
@@ -422,9 +435,10 @@ struct ReconA : PassBase {
                     const int yo = y - y0;
                     if (kxc + q < nx && yo >= 0 && yo < ny_out) __stcs(tb + (size_t)yo * nx + kxc + q, v);
                 }
-                cluster_sync();   // the peers have read these rows before the next slice rewrites them
+                cluster_arrive();   // this thread has read the cluster's rows of slice b
             }
         }
+        if constexpr (CS > 1) cluster_wait();   // no CTA leaves while a peer reads its rows
     }
 };
 
@@ -625,13 +639,17 @@ enum RowMode {
 
 __device__ __forceinline__ float2 amplitude_replace(float2 u, float s) {
     const float n2 = fmaf(u.x, u.x, u.y * u.y);
-    if (n2 == 0.0f) {
-        if (u.x == 0.0f && u.y == 0.0f) return make_float2(s, 0.0f);   // angle(0) == 0
-    }
     // 1/|u| from the hardware reciprocal square root where |u|^2 is a normal,
-    // representable float; rhypotf (scaled) for the rest
-    const float inv = (n2 > 1e-36f && n2 < 1e36f) ? rsqrtf(n2) : rhypotf(u.x, u.y);
-    return make_float2(u.x * inv * s, u.y * inv * s);
+    // representable float (one test on the common path); rhypotf (scaled) for
+    // the rest, and angle(0) == 0 for a zero field
+    float k;
+    if (__builtin_expect(n2 > 1e-36f && n2 < 1e36f, 1)) {
+        k = rsqrtf(n2) * s;
+    } else {
+        if (u.x == 0.0f && u.y == 0.0f) return make_float2(s, 0.0f);
+        k = rhypotf(u.x, u.y) * s;
+    }
+    return make_float2(u.x * k, u.y * k);
 }
 
 // Rows y of [y][kx] data (row length nx).
@@ -774,6 +792,11 @@ struct GsRowMidT : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
+        run_blocks<N, RF, false>(smem, r, j);
+    }
+
+    template <int N, bool RF, bool RESID>
+    __device__ __forceinline__ void run_blocks(unsigned char *smem, int r, int j) const {
         static_assert(RF, "rows-fastest launch");
         using SN = S<N>;
         constexpr int E = SN::E, ROWS = SN::ROWS;
@@ -813,10 +836,11 @@ struct GsRowMidT : PassBase {
             const float *hr = reinterpret_cast<const float *>(base + FB) + (size_t)r * HS;
             const int y = rb * ROWS + r;
             const bool valid = y < nrows;
+            const float2 *tw = opaque(this->tw);   // twiddles are re-read per block, not held in registers
             fft_row<N, E, true, true>(xr, j, tw, [&](int, int x) -> float2 { return xr[x]; },
                                       [&](int, int x, float2 v) -> float2 {
                                           const float s = hr[x];
-                                          if (resid != nullptr && valid) {
+                                          if (RESID && valid) {
                                               const double a = sqrt((double)v.x * v.x + (double)v.y * v.y) - (double)s;
                                               acc0 += a * a;
                                               acc1 += (double)s * s;
@@ -828,7 +852,7 @@ struct GsRowMidT : PassBase {
                                      if (valid) dst[(size_t)kx * nrows + y] = v;
                                  });
         }
-        if (resid != nullptr) {
+        if (RESID) {
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
@@ -839,6 +863,16 @@ struct GsRowMidT : PassBase {
                 atomicAdd(resid + 1, acc1);
             }
         }
+    }
+};
+
+// The pass that also accumulates the GS residual (the last plane-2 pass of a
+// call that asks for it): its own kernel, so that the FP64 accumulators do not
+// enlarge the register budget of every other row pass.
+struct GsRowMidTResid : GsRowMidT {
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
+        run_blocks<N, RF, true>(smem, r, j);
     }
 };
 

@@ -76,6 +76,14 @@ __device__ __forceinline__ uint32_t cluster_ctarank() {
 __device__ __forceinline__ void cluster_sync() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+// The two halves of cluster_sync, for work between a thread's arrival and its
+// wait.  Each thread alternates arrive and wait.
+__device__ __forceinline__ void cluster_arrive() {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
 // The shared::cluster address of shared-memory address `saddr` in CTA `rank` of the cluster.
 __device__ __forceinline__ uint32_t map_to_rank(uint32_t saddr, uint32_t rank) {

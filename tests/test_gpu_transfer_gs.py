@@ -98,7 +98,7 @@ def test_gs_golden(ph, cuda, golden):
     assert abs(float(res) - float(g["gs_resid"])) < 1e-4 * max(1.0, float(g["gs_resid"]))
 
 
-@pytest.mark.parametrize("n,iters", [(1, 2), (8, 3), (128, 4), (512, 3), (96, 3), (768, 2)])
+@pytest.mark.parametrize("n,iters", [(1, 2), (8, 3), (128, 4), (512, 3), (96, 3), (768, 2), (1024, 3)])
 def test_gs_matches_oracle(ph, cuda, n, iters):
     rng = np.random.default_rng(n)
     h1 = rng.uniform(0.1, 1.0, (n, n)).astype(np.float32)
@@ -122,6 +122,17 @@ def test_gs_real_holograms(ph, cuda, golden):
                                    ph.CuTransfer(to_dev(tpi, cuda)), 20, n)
     assert tuple(u.data.shape) == (n, n) and u.data.dtype == torch.complex64
     assert rel_l2(to_np(u.data), ref.phase_retrieval_holo(h1, h2, tp, tpi, 20, n)) < REL_L2
+
+
+@pytest.mark.parametrize("n", [64, 1024])
+def test_gs_zero_field(ph, cuda, n):
+    """A zero transfer makes every propagated field exactly zero; angle(0) == 0
+    (holofunc.jl:115-125), so each amplitude replacement gives sqrt(I) + 0i."""
+    h1 = torch.rand((n, n), device=cuda) + 0.1
+    h2 = torch.rand((n, n), device=cuda) + 0.1
+    z = ph.CuTransfer(torch.zeros((n, n), dtype=torch.complex64, device=cuda))
+    u = ph.cu_phase_retrieval_holo(h1, h2, z, z, 3, n)
+    assert torch.equal(u.data, torch.complex(torch.sqrt(h1), torch.zeros_like(h1)))
 
 
 def test_gs_zero_iterations_and_sizes(ph, cuda):
