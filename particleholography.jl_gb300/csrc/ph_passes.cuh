@@ -637,17 +637,24 @@ enum RowMode {
     ROW_INV = 2,      // inverse FFT -> natural store
 };
 
+// s / |u| where |u|^2 is not a normal, representable float: rhypotf (scaled);
+// -1 for a zero field.  Out of line, so that the rare path takes no registers
+// from the transforms around the common one.
+static __device__ __noinline__ float amplitude_scale_slow(float2 u, float s) {
+    if (u.x == 0.0f && u.y == 0.0f) return -1.0f;
+    return rhypotf(u.x, u.y) * s;
+}
+// s u / |u|, and (s, 0) for u == 0 (angle(0) == 0).  1/|u| from the hardware
+// reciprocal square root where |u|^2 is a normal, representable float (one
+// test on the common path).
 __device__ __forceinline__ float2 amplitude_replace(float2 u, float s) {
     const float n2 = fmaf(u.x, u.x, u.y * u.y);
-    // 1/|u| from the hardware reciprocal square root where |u|^2 is a normal,
-    // representable float (one test on the common path); rhypotf (scaled) for
-    // the rest, and angle(0) == 0 for a zero field
     float k;
     if (__builtin_expect(n2 > 1e-36f && n2 < 1e36f, 1)) {
         k = rsqrtf(n2) * s;
     } else {
-        if (u.x == 0.0f && u.y == 0.0f) return make_float2(s, 0.0f);
-        k = rhypotf(u.x, u.y) * s;
+        k = amplitude_scale_slow(u, s);
+        if (k < 0.0f) return make_float2(s, 0.0f);
     }
     return make_float2(u.x * k, u.y * k);
 }

@@ -135,6 +135,22 @@ def test_gs_zero_field(ph, cuda, n):
     assert torch.equal(u.data, torch.complex(torch.sqrt(h1), torch.zeros_like(h1)))
 
 
+@pytest.mark.parametrize("n", [64, 1024])
+def test_gs_tiny_field(ph, cuda, n):
+    """Transfers scaled by 1e-20 make |u|^2 ~ 1e-40 (subnormal), so every
+    amplitude replacement takes its scaled path; the phases, and so the
+    result, still match the oracle."""
+    rng = np.random.default_rng(5)
+    h1 = rng.uniform(0.1, 1.0, (n, n)).astype(np.float32)
+    h2 = rng.uniform(0.1, 1.0, (n, n)).astype(np.float32)
+    d = ref.transfer_sqrt_arr(n, LAM, DX)
+    tp = (ref.transfer(5000.0, n, LAM, d) * np.float32(1e-20)).astype(np.complex64)
+    tpi = (ref.transfer(-5000.0, n, LAM, d) * np.float32(1e-20)).astype(np.complex64)
+    u = ph.cu_phase_retrieval_holo(to_dev(h1, cuda), to_dev(h2, cuda), ph.CuTransfer(to_dev(tp, cuda)),
+                                   ph.CuTransfer(to_dev(tpi, cuda)), 3, n)
+    assert rel_l2(to_np(u.data), ref.phase_retrieval_holo(h1, h2, tp, tpi, 3, n)) < REL_L2
+
+
 def test_gs_zero_iterations_and_sizes(ph, cuda):
     n = 16
     h = torch.rand((n, n), device=cuda)
