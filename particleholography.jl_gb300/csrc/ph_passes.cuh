@@ -76,6 +76,8 @@ struct PassBase {
     static constexpr int EPT = 16;
     static constexpr int TT = 512;    // target threads per CTA
     static constexpr int RTS = 512;   // resident threads per SM the register budget allows
+    template <int N>
+    static constexpr int rts() { return RTS; }
     template <int N, bool ROW_FAST>
     static constexpr size_t smem() { return Shape<N, EPT, TT>::template smem_bytes<ROW_FAST>(); }
     // Persistent passes loop over row blocks; their grid is the resident CTA count.
@@ -113,10 +115,10 @@ __device__ __forceinline__ float2 *xrow(unsigned char *base, int r) {
     return reinterpret_cast<float2 *>(base) + (size_t)r * Shape<N, EPT, TT>::template stride<ROW_FAST>();
 }
 
-// Register budget: RTS resident threads per SM.
+// Register budget: rts<N>() resident threads per SM.
 template <int N, class Body>
 constexpr int min_blocks() {
-    return cmax(1, Body::RTS / Shape<N, Body::EPT, Body::TT>::THREADS);
+    return cmax(1, Body::template rts<N>() / Shape<N, Body::EPT, Body::TT>::THREADS);
 }
 
 template <int N, bool ROW_FAST, class Body>
@@ -473,6 +475,12 @@ template <int EPI>
 struct ReconB : PassBase {
     static constexpr int TT = 128;
     static constexpr int RTS = PH_RECONB_RTS;
+    // 3 * 2^a lengths hold 24 values per thread and their running minima:
+    // 168 registers, three CTAs per SM.  Per launch at 1536 and 3072 that is
+    // 28 % faster than five CTAs at 96 registers (spilling ~480 bytes) and
+    // 9-12 % faster than four at 128 (spilling ~150 bytes).
+    template <int N>
+    static constexpr int rts() { return plan_pow2(N) ? RTS : 384; }
     const float2 *t;                 // [batch][rows][nx]
     const float2 *tw;
     unsigned long long *proj64;      // [rows_out][nx_out] or null
