@@ -274,19 +274,24 @@ struct ReconA : PassBase {
     int k0;                // global slice index of batch slot 0
     int nbatch, group;     // slices in the batch, slices per CTA
 
-    // Two staged forms.
-    //  chain: shared memory holds, per row, X_k and Hdz as two float2 rows;
-    //    every slice reads X_k and advances it in place, X_{k+1} = X_k Hdz (the
-    //    reference's cumulative product).  The CTA computes X at its first
-    //    slice directly from the state, so each product chain spans at most
-    //    `group` slices.
-    //  direct: the state rows are staged by bulk copy and every slice
-    //    evaluates Hdz^k from them.
-    // The chain saves the per-voxel sin/cos; the direct form moves fewer
-    // shared-memory bytes per voxel and needs fewer registers.  Measured per
-    // pass A launch, chain against direct: 2048 3.7 % faster; 1024 18 % slower
-    // (register spills); 4096 2.7 % slower (its cluster store competes for
-    // shared-memory bandwidth).  Other lengths keep the direct form.
+    // Staged forms, the first that fits the CTA's shared memory beside the
+    // exchange rows:
+    //  FORM_CHAIN: per row, X_k and Hdz as two float2 rows; every slice reads
+    //    X_k and advances it in place, X_{k+1} = X_k Hdz (the reference's
+    //    cumulative product).  The CTA computes X at its first slice directly
+    //    from the state, so each product chain spans at most `group` slices.
+    //  FORM_STATE: the state rows, staged by bulk copy; every slice evaluates
+    //    Hdz^k from them.
+    //  FORM_X0: only X0 (8 of the state's 16 bytes) staged; the phase rate
+    //    and |Hdz| - 1 come from L2 every slice.  (3 * 2^a lengths, whose
+    //    24-value threads give a CTA 8 rows: their full state does not fit.)
+    //  FORM_NONE: the whole state from L2 every slice.
+    // The chain saves the per-voxel sin/cos; the direct forms move fewer
+    // shared-memory bytes per voxel and need fewer registers.  Measured per
+    // pass A launch, chain against the staged state: 2048 3.7 % faster; 1024
+    // 18 % slower (register spills); 4096 2.7 % slower (its cluster store
+    // competes for shared-memory bandwidth).  Other lengths keep the direct form.
+    enum { FORM_NONE = 0, FORM_X0 = 1, FORM_STATE = 2, FORM_CHAIN = 3 };
     template <int N>
     static constexpr bool chain() {
         return PH_RECONA_CHAIN >= 0 ? PH_RECONA_CHAIN != 0 : N == 2048;
@@ -303,18 +308,27 @@ struct ReconA : PassBase {
         return (dense + 127) / 128 * 128 + (16 * (8 / (R < 8 ? R : 8))) % 128;
     }
     template <int N, bool RF>
-    static constexpr size_t stage_bytes() {   // staged rows (+ the bulk-copy barrier of the direct form)
-        return chain<N>() ? round128((size_t)2 * Shape<N, EPT, TT>::ROWS * rec_stride<N, RF>() * 8)
-                          : round128((size_t)Shape<N, EPT, TT>::ROWS * state_stride<N>() + 8);
+    static constexpr size_t form_bytes(int f) {   // staged rows (+ the bulk-copy barrier of FORM_STATE)
+        using S = Shape<N, EPT, TT>;
+        return f == FORM_CHAIN ? round128((size_t)2 * S::ROWS * rec_stride<N, RF>() * 8)
+             : f == FORM_STATE ? round128((size_t)S::ROWS * state_stride<N>() + 8)
+             : f == FORM_X0    ? round128((size_t)S::ROWS * rec_stride<N, RF>() * 8)
+                               : 0;
     }
-    // Staged when the staged rows and the exchange rows fit the CTA's shared memory.
     template <int N, bool RF>
-    static constexpr bool staged() {
-        return stage_bytes<N, RF>() + Shape<N, EPT, TT>::template smem_bytes<RF>() <= kSmemMax;
+    static constexpr bool fits(int f) {
+        return form_bytes<N, RF>(f) + Shape<N, EPT, TT>::template smem_bytes<RF>() <= kSmemMax;
+    }
+    template <int N, bool RF>
+    static constexpr int form() {
+        return (chain<N>() && fits<N, RF>(FORM_CHAIN)) ? FORM_CHAIN
+             : fits<N, RF>(FORM_STATE)                ? FORM_STATE
+             : fits<N, RF>(FORM_X0)                   ? FORM_X0
+                                                      : FORM_NONE;
     }
     template <int N, bool RF>
     static constexpr size_t stage_total() {
-        return staged<N, RF>() ? stage_bytes<N, RF>() : 0;
+        return form_bytes<N, RF>(form<N, RF>());
     }
     template <int N, bool RF>
     static constexpr size_t smem() {
@@ -334,7 +348,7 @@ struct ReconA : PassBase {
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
         using S = Shape<N, EPT, TT>;
         constexpr int ROWS = S::ROWS;
-        constexpr bool CHAIN = staged<N, RF>() && chain<N>();
+        constexpr int FORM = form<N, RF>();
         unsigned char *xbase = smem + stage_total<N, RF>();
         constexpr int CS = cluster<N>();
         // The CTAs of one row block (its `gridDim.y` slice groups) are consecutive
@@ -349,7 +363,7 @@ struct ReconA : PassBase {
         const int b1 = min(b0 + group, nbatch);
         const float4 *srow = state + (size_t)(valid ? kx : 0) * N;
         float2 *xs = nullptr, *hs = nullptr;
-        if constexpr (CHAIN) {
+        if constexpr (FORM == FORM_CHAIN) {
             constexpr int XS = rec_stride<N, RF>();
             xs = reinterpret_cast<float2 *>(smem) + (size_t)r * XS;
             hs = reinterpret_cast<float2 *>(smem) + (size_t)(ROWS + r) * XS;
@@ -370,7 +384,14 @@ struct ReconA : PassBase {
                 xs[col] = x;
                 hs[col] = h;
             }
-        } else if constexpr (staged<N, RF>()) {
+        } else if constexpr (FORM == FORM_X0) {
+            xs = reinterpret_cast<float2 *>(smem) + (size_t)r * rec_stride<N, RF>();
+#pragma unroll
+            for (int q = 0; q < S::E; ++q) {
+                const int col = in_col<N, S::E>(j, q);   // the columns this thread's first stage reads
+                xs[col] = valid ? *reinterpret_cast<const float2 *>(srow + col) : make_float2(0.0f, 0.0f);
+            }
+        } else if constexpr (FORM == FORM_STATE) {
             constexpr size_t SS = state_stride<N>();
             uint64_t *bar = reinterpret_cast<uint64_t *>(smem + ROWS * SS);
             if (threadIdx.x == 0) {
@@ -393,10 +414,14 @@ struct ReconA : PassBase {
             const uint32_t k = (uint32_t)(k0 + b);
             float2 *tb = t + (size_t)b * ny_out * nx;
             auto load = [&](int, int ky) -> float2 {
-                if constexpr (CHAIN) {
+                if constexpr (FORM == FORM_CHAIN) {
                     const float2 x = xs[ky];   // written by this thread only
                     xs[ky] = cmul(x, hs[ky]);
                     return x;
+                } else if constexpr (FORM == FORM_X0) {
+                    const float2 x0 = xs[ky];   // written by this thread only
+                    const float2 pm = __ldg(reinterpret_cast<const float2 *>(srow + ky) + 1);
+                    return direct(make_float4(x0.x, x0.y, pm.x, pm.y), k);
                 } else {
                     return direct(srow[ky], k);
                 }
