@@ -409,7 +409,7 @@ struct ReconA : PassBase {
             srow = reinterpret_cast<const float4 *>(smem + (size_t)r * SS);
         }
         float2 *xr = xrow<N, EPT, TT, RF>(xbase, r);
-        if constexpr (CS > 1) cluster_arrive();   // pairs with the first slice's wait
+        if constexpr (CS > 1) cluster_arrive_relaxed();   // pairs with the first slice's wait
         for (int b = b0; b < b1; ++b) {
             const uint32_t k = (uint32_t)(k0 + b);
             float2 *tb = t + (size_t)b * ny_out * nx;
@@ -462,7 +462,11 @@ struct ReconA : PassBase {
                     const int yo = y - y0;
                     if (kxc + q < nx && yo >= 0 && yo < ny_out) __stcs(tb + (size_t)yo * nx + kxc + q, v);
                 }
-                cluster_arrive();   // this thread has read the cluster's rows of slice b
+                // This thread has read the cluster's rows of slice b: the stores
+                // above consumed every loaded value, so the loads are complete
+                // and the arrival orders nothing.  (A release arrival waited for
+                // those global stores: 10 % slower at 4096.)
+                cluster_arrive_relaxed();
             }
         }
         if constexpr (CS > 1) cluster_wait();   // no CTA leaves while a peer reads its rows

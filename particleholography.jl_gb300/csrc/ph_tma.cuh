@@ -78,12 +78,16 @@ __device__ __forceinline__ void cluster_sync() {
 }
 // The two halves of cluster_sync, for work between a thread's arrival and its
 // wait.  Each thread alternates arrive and wait.
-__device__ __forceinline__ void cluster_arrive() {
-    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-}
 __device__ __forceinline__ void cluster_wait() {
     asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+// An arrival that orders no memory access (no release fence, which would
+// wait for this thread's outstanding global stores): for signalling that
+// loads whose values the thread has already used are complete.
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+
 
 // The shared::cluster address of shared-memory address `saddr` in CTA `rank` of the cluster.
 __device__ __forceinline__ uint32_t map_to_rank(uint32_t saddr, uint32_t rank) {
