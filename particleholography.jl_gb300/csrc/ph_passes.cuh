@@ -725,18 +725,24 @@ struct GsRow : PassBase {
             });
         } else {
             double acc0 = 0.0, acc1 = 0.0;
-            fft_row<N, E, true, true>(srow, j, tw, ld, [&](int, int x, float2 v) -> float2 {
-                if (!valid) return make_float2(0.f, 0.f);
-                const float s = sqrtf(holo[(size_t)y * N + x]);
-                if (resid != nullptr) {
-                    const double a = sqrt((double)v.x * v.x + (double)v.y * v.y) - (double)s;
-                    acc0 += a * a;
-                    acc1 += (double)s * s;
+            // the amplitude replacement passes between the transforms in
+            // registers (columns j + s P, as in GsRowMidT)
+            float2 mid[E];
+            fft_row<N, E, true>(srow, j, tw, ld, [&](int, int x, float2 v) {
+                float2 w = make_float2(0.f, 0.f);
+                if (valid) {
+                    const float s = sqrtf(holo[(size_t)y * N + x]);
+                    if (resid != nullptr) {
+                        const double a = sqrt((double)v.x * v.x + (double)v.y * v.y) - (double)s;
+                        acc0 += a * a;
+                        acc1 += (double)s * s;
+                    }
+                    w = amplitude_replace(v, s);
                 }
-                return amplitude_replace(v, s);
+                mid[(x - j) / S::P] = w;
             });
             fft_row<N, E, false>(
-                srow, j, tw, [&](int, int x) -> float2 { return srow[spad(x)]; },
+                srow, j, tw, [&](int, int x) -> float2 { return mid[(x - j) / S::P]; },
                 [&](int, int kx, float2 v) {
                     if (valid) dst[(size_t)kx * nrows + y] = v;
                 });
@@ -776,16 +782,21 @@ struct GsCol : PassBase {
         const bool valid = kx < nx;
         const int sx = valid ? shift_idx(kx, nx) : 0;
         const float2 *in = src + (size_t)(valid ? kx : 0) * N;
-        fft_row<N, E, false, true>(
+        // the product passes between the transforms in registers (this
+        // thread's columns j + s P, as in GsColT)
+        float2 mid[E];
+        fft_row<N, E, false>(
             srow, j, tw, [&](int, int y) -> float2 { return valid ? in[y] : make_float2(0.f, 0.f); },
-            [&](int, int ky, float2 v) -> float2 {
-                if (!valid) return make_float2(0.f, 0.f);
-                const size_t c = (size_t)shift_idx(ky, N) * nx + sx;
-                if (mask != nullptr) return cscale(v, mask[c] * scale);
-                return cscale(cmul(v, h[c]), scale);
+            [&](int, int ky, float2 v) {
+                float2 w = make_float2(0.f, 0.f);
+                if (valid) {
+                    const size_t c = (size_t)shift_idx(ky, N) * nx + sx;
+                    w = mask != nullptr ? cscale(v, mask[c] * scale) : cscale(cmul(v, h[c]), scale);
+                }
+                mid[(ky - j) / S::P] = w;
             });
         fft_row<N, E, true>(
-            srow, j, tw, [&](int, int ky) -> float2 { return srow[spad(ky)]; },
+            srow, j, tw, [&](int, int ky) -> float2 { return mid[(ky - j) / S::P]; },
             [&](int, int y, float2 v) {
                 if (valid) dst[(size_t)y * nx + kx] = v;
             });
@@ -881,17 +892,22 @@ struct GsRowMidT : PassBase {
             const int y = rb * ROWS + r;
             const bool valid = y < nrows;
             const float2 *tw = opaque(this->tw);   // twiddles are re-read per block, not held in registers
-            fft_row<N, E, true, true>(xr, j, tw, [&](int, int x) -> float2 { return xr[x]; },
-                                      [&](int, int x, float2 v) -> float2 {
-                                          const float s = hr[x];
-                                          if (RESID && valid) {
-                                              const double a = sqrt((double)v.x * v.x + (double)v.y * v.y) - (double)s;
-                                              acc0 += a * a;
-                                              acc1 += (double)s * s;
-                                          }
-                                          return amplitude_replace(v, s);
-                                      });
-            fft_row<N, E, false>(xr, j, tw, [&](int, int x) -> float2 { return xr[spad(x)]; },
+            // The inverse transform's last stage leaves this thread the columns
+            // j + s P (s < E), the very columns the forward transform's first
+            // stage reads: the amplitude replacement passes between them in
+            // registers.
+            float2 mid[E];
+            fft_row<N, E, true>(xr, j, tw, [&](int, int x) -> float2 { return xr[x]; },
+                                [&](int, int x, float2 v) {
+                                    const float s = hr[x];
+                                    if (RESID && valid) {
+                                        const double a = sqrt((double)v.x * v.x + (double)v.y * v.y) - (double)s;
+                                        acc0 += a * a;
+                                        acc1 += (double)s * s;
+                                    }
+                                    mid[(x - j) / SN::P] = amplitude_replace(v, s);
+                                });
+            fft_row<N, E, false>(xr, j, tw, [&](int, int x) -> float2 { return mid[(x - j) / SN::P]; },
                                  [&](int, int kx, float2 v) {
                                      if (valid) dst[(size_t)kx * nrows + y] = v;
                                  });
@@ -1012,14 +1028,25 @@ struct GsColT : PassBase {
             const int kx = rb * ROWS + r;
             const bool valid = kx < nx;
             auto go = [&](const auto twv) {
-                fft_row<N, E, false, true>(xr, j, twv, [&](int, int y) -> float2 { return xr[y]; },
-                                           [&](int, int ky, float2 v) -> float2 { return cmul(v, hr[ky]); });
-                // the transform ended with a barrier: the transfer rows are free
-                if (HT_EARLY && threadIdx.x == 0 && next < nblocks) issue_ht(next);
-                fft_row<N, E, true>(xr, j, twv, [&](int, int ky) -> float2 { return xr[spad(ky)]; },
-                                    [&](int, int y, float2 v) {
-                                        if (valid) dst[(size_t)y * nx + kx] = v;
-                                    });
+                // The forward transform's last stage leaves this thread the columns
+                // j + s P (s < E), the very columns the inverse transform's first
+                // stage reads: the product with the transfer passes between them
+                // in registers.
+                float2 mid[E];
+                fft_row<N, E, false>(xr, j, twv, [&](int, int y) -> float2 { return xr[y]; },
+                                     [&](int, int ky, float2 v) { mid[(ky - j) / SN::P] = cmul(v, hr[ky]); });
+                int nsync = 0;
+                const auto sync = [&]() {
+                    __syncthreads();
+                    // first barrier of the inverse transform: every thread has read
+                    // the transfer rows, so the next block's may come in
+                    if (nsync++ == 0 && HT_EARLY && threadIdx.x == 0 && next < nblocks) issue_ht(next);
+                };
+                fft_row_sync<N, E, true>(xr, j, twv, [&](int, int ky) -> float2 { return mid[(ky - j) / SN::P]; },
+                                         [&](int, int y, float2 v) {
+                                             if (valid) dst[(size_t)y * nx + kx] = v;
+                                         },
+                                         sync);
             };
             if constexpr (TWS) go(tws);
             else go(opaque(this->tw));   // twiddles are re-read per block, not held in registers
