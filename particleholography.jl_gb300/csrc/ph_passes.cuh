@@ -32,6 +32,9 @@
 #ifndef PH_RECONB_RTS
 #define PH_RECONB_RTS 640
 #endif
+#ifndef PH_RECONA_CHAIN_SMALL
+#define PH_RECONA_CHAIN_SMALL 0
+#endif
 #ifndef PH_RECONA_CHAIN
 #define PH_RECONA_CHAIN -1   // pass A product chain: -1 per length (chain<N>()), 0 never, 1 always
 #endif
@@ -294,7 +297,7 @@ struct ReconA : PassBase {
     enum { FORM_NONE = 0, FORM_X0 = 1, FORM_STATE = 2, FORM_CHAIN = 3 };
     template <int N>
     static constexpr bool chain() {
-        return PH_RECONA_CHAIN >= 0 ? PH_RECONA_CHAIN != 0 : N == 2048;
+        return PH_RECONA_CHAIN >= 0 ? PH_RECONA_CHAIN != 0 : (N == 2048 || (PH_RECONA_CHAIN_SMALL && N <= 512));
     }
     template <int N, bool RF>
     static constexpr int rec_stride() {   // float2 between rows: conflict-free for the load pattern
