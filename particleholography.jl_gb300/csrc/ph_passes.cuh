@@ -32,9 +32,6 @@
 #ifndef PH_RECONB_RTS
 #define PH_RECONB_RTS 640
 #endif
-#ifndef PH_RECONA_CHAIN_SMALL
-#define PH_RECONA_CHAIN_SMALL 0
-#endif
 #ifndef PH_RECONA_CHAIN
 #define PH_RECONA_CHAIN -1   // pass A product chain: -1 per length (chain<N>()), 0 never, 1 always
 #endif
@@ -291,13 +288,15 @@ struct ReconA : PassBase {
     //  FORM_NONE: the whole state from L2 every slice.
     // The chain saves the per-voxel sin/cos; the direct forms move fewer
     // shared-memory bytes per voxel and need fewer registers.  Measured per
-    // pass A launch, chain against the staged state: 2048 3.7 % faster; 1024
-    // 18 % slower (register spills); 4096 2.7 % slower (its cluster store
-    // competes for shared-memory bandwidth).  Other lengths keep the direct form.
+    // pass A launch, chain against the staged state: 2048 3.7 % and 512 2.7 %
+    // faster; 1024 18 % slower (register spills); 4096 6 % slower (its cluster
+    // store competes for shared-memory bandwidth); 256 22 % slower (slice groups
+    // of 6 slices do not repay the chain's start).  Other lengths keep the
+    // direct form.
     enum { FORM_NONE = 0, FORM_X0 = 1, FORM_STATE = 2, FORM_CHAIN = 3 };
     template <int N>
     static constexpr bool chain() {
-        return PH_RECONA_CHAIN >= 0 ? PH_RECONA_CHAIN != 0 : (N == 2048 || (PH_RECONA_CHAIN_SMALL && N <= 512));
+        return PH_RECONA_CHAIN >= 0 ? PH_RECONA_CHAIN != 0 : (N == 2048 || N == 512);
     }
     template <int N, bool RF>
     static constexpr int rec_stride() {   // float2 between rows: conflict-free for the load pattern
