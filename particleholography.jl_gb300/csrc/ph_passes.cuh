@@ -248,16 +248,16 @@ struct SpectrumCols : PassBase {
 // and |Hdz|^k ~ 1 + k (|Hdz| - 1).
 //
 // A CTA transforms `group` consecutive slices from rows staged in shared
-// memory once (the two forms are described at `chain`).  Staged rows are
-// spaced so that the accesses of one phase of lanes (ROWS rows x consecutive
-// columns) fall on distinct banks.
+// memory once (the staging forms are described at FORM_CHAIN .. FORM_NONE).
+// Staged rows are spaced so that the accesses of one phase of lanes (ROWS rows
+// x consecutive columns) fall on distinct banks.
 //
 // The transposed store writes 4 consecutive kx (one 32-byte sector) per y.
 // Where a CTA holds fewer than 4 rows (N >= 4096), 4 / ROWS CTAs form a
 // thread-block cluster: each leaves its transformed rows in shared memory,
 // and after a cluster barrier each stores a 1 / (4 / ROWS) share of the y
 // range for all 4 rows, reading its peers' rows through distributed shared
-// memory.  (Stores of 2 consecutive kx, 16 bytes, ran 3x slower.)
+// memory.  (Stores of 2 consecutive kx, 16 bytes, ran 2-4x slower.)
 struct ReconA : PassBase {
     // 4 rows of 128 threads at N = 2048: one CTA per SM.  (One row per CTA in
     // clusters of 4, or two in clusters of 2, measured 65 % / 59 % slower.)
