@@ -54,6 +54,10 @@ CONFIGS = {
     "p2": dict(n=2048, slices=64, dz=200.0, z0=5000.0, discs=800, dmin=10.0, dmax=60.0, zmin=5000.0,
                zmax=100000.0, gs_iters=2, gs_sep=5000.0, threshold=0.1, seed=2,
                workload="gs2048_pr2_recon64_profile"),
+    # the 4096^2 workload cut to one 16-slice batch, for kernel captures of pass A in clusters
+    "p3": dict(n=4096, slices=16, dz=(200000.0 - 5000.0) / 1024, z0=5000.0, discs=3000, dmin=10.0, dmax=60.0,
+               zmin=5000.0, zmax=200000.0, gs_iters=0, gs_sep=0.0, threshold=0.1, seed=3,
+               workload="gabor4096_recon16_profile"),
 }
 # Mixed batch: (n_fast, n_slow, count) size classes; per item slices ~ U{32..512} and
 # dz ~ U(0.1, 0.5) mm drawn from numpy PCG64(1000 + i); reconstructed from z0 = 5 mm.
