@@ -19,6 +19,9 @@ export cu_transfer_sqrt_arr, cu_transfer, cu_gabor_wavefront, cu_phase_retrieval
        cu_asm_prop!, cu_2d_pad, cu_get_reconst_vol_and_xyprojection_padded,
        cu_connected_component_labeling, count_labels, cu_find_valid_labels,
        cu_get_reconst_xyprojection_argmin, cu_apply_low_pass_filter!, cu_apply_low_pass_filter,
+       cu_rectangle_filter, cu_super_gaussian_filter, cu_get_reconst_xyprojection_lpf,
+       cu_get_reconst_binary_vol, slice_bounding_rectangles, cu_reconst_subvolumes,
+       cu_make_background_mode, pad_with_mean,
        ReconBatch, run!, Server, submit!, poll
 
 const libphgb300 = get(ENV, "PHGB300_LIB", joinpath(@__DIR__, "..", "libphgb300.so"))
@@ -219,6 +222,132 @@ function cu_find_valid_labels(labels::CuArray{UInt32,2})
     _, roots = _roots(labels, c)
     return roots[1:c]
 end
+
+# ---- frequency_filters.jl ------------------------------------------------------------
+
+for (name, sym) in ((:cu_rectangle_filter, :ph_lpf_rectangle), (:cu_super_gaussian_filter, :ph_lpf_super_gaussian))
+    @eval function $name(prop_dist::AbstractFloat, wavlen::AbstractFloat, imglen::Int, pixel_picth::AbstractFloat)
+        arr = CuArray{Float32}(undef, imglen, imglen)
+        _check(ccall(($(QuoteNode(sym)), libphgb300), Int32,
+                     (Ptr{Cvoid}, CuPtr{Float32}, Int32, Float64, Float64, Float64, Ptr{Cvoid}),
+                     _ctx(), arr, imglen, prop_dist, wavlen, pixel_picth, _stream()))
+        return CuLowPassFilter(arr)
+    end
+end
+
+# cu_apply_low_pass_filter then cu_get_reconst_xyprojection, the filter folded into
+# the spectrum (no FFT pair); also returns the argmin depth (0-based, Int32).
+function cu_get_reconst_xyprojection_lpf(light_field::CuWavefront{ComplexF32}, transfer_front::CuTransfer{ComplexF32},
+                                         transfer_dz::CuTransfer{ComplexF32}, lpf::CuLowPassFilter, slices::Int)
+    n1, n2 = size(light_field.data)
+    @assert size(transfer_front.data) == size(transfer_dz.data) == size(lpf.data) == (n1, n2) "All arrays must have the same size."
+    proj = CuArray{Float32}(undef, n1, n2)
+    amin = CuArray{Int32}(undef, n1, n2)
+    _check(ccall((:ph_reconst_xyproj_lpf, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{Float32}, CuPtr{Int32}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CuPtr{ComplexF32},
+                  CuPtr{Float32}, Int32, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), proj, amin, light_field.data, transfer_front.data, transfer_dz.data, lpf.data, n1, n2, slices,
+                 _stream()))
+    return proj, amin
+end
+
+# ---- particle_detection.jl (the device side of particle_bounding_boxes) ----------------
+
+# cu_get_reconst_vol(..., Float32) .<= threshold in one pass, without the Float32 volume.
+function cu_get_reconst_binary_vol(light_field::CuWavefront{ComplexF32}, transfer_front::CuTransfer{ComplexF32},
+                                   transfer_dz::CuTransfer{ComplexF32}, slices::Int, threshold::Real)
+    n1, n2 = size(light_field.data)
+    @assert size(transfer_front.data) == size(transfer_dz.data) == (n1, n2) "All arrays must have the same size."
+    vol = CuArray{Bool}(undef, n1, n2, slices)
+    _check(ccall((:ph_reconst_binary_vol, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{Bool}, Float32, CuPtr{Float32}, CuPtr{ComplexF32}, CuPtr{ComplexF32},
+                  CuPtr{ComplexF32}, Int32, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), vol, threshold, CU_NULL, light_field.data, transfer_front.data, transfer_dz.data, n1, n2,
+                 slices, _stream()))
+    return vol
+end
+
+# For every slice of a binary volume, what
+# get_bounding_rectangles(Array(cu_connected_component_labeling(vol[:, :, k])),
+#                         cu_find_valid_labels(...))
+# returns, (x_min, y_min, x_max, y_max) per component in root order: all slices
+# labelled in one launch set and boxed on the device.  The loop of
+# particle_bounding_boxes then only merges neighbourhoods on the host.
+function slice_bounding_rectangles(d_bin_vol::CuArray{Bool,3})
+    rows, cols, slices = size(d_bin_vol)
+    labels = CuArray{UInt32}(undef, rows, cols, slices)
+    _check(ccall((:ph_ccl_batch, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{UInt32}, CuPtr{Cvoid}, Int32, Int64, Int64, Int64, Ptr{Cvoid}),
+                 _ctx(), labels, d_bin_vol, PH_BOOL, slices, rows, cols, _stream()))
+    count = Ref{Int64}(0)
+    boxes_call(buf, cap) = _check(ccall((:ph_ccl_boxes, libphgb300), Int32,
+                                        (Ptr{Cvoid}, Ptr{Int64}, Int64, Ref{Int64}, CuPtr{UInt32}, Int64, Int64, Int64,
+                                         Ptr{Cvoid}),
+                                        _ctx(), buf, cap, count, labels, slices, rows, cols, _stream()))
+    boxes_call(C_NULL, 0)
+    boxes = Vector{Int64}(undef, 5 * count[])
+    boxes_call(boxes, count[])
+    out = [NTuple{4,Int}[] for _ in 1:slices]
+    per = rows * cols
+    for b in 1:count[]
+        root, x0, y0, x1, y1 = boxes[5b-4], boxes[5b-3], boxes[5b-2], boxes[5b-1], boxes[5b]
+        push!(out[div(root - 1, per) + 1], (x0, y0, x1, y1))
+    end
+    return out
+end
+
+# The N0f8 sub-volumes particle_coordinates / particle_coor_diams cut out of
+# cu_get_reconst_vol(..., N0f8): d_vol[y_min:y_max, x_min:x_max, z_min:z_max] for
+# each box (x_min, y_min, z_min, x_max, y_max, z_max) (particle_bbs order,
+# 1-based inclusive), without the volume; only the covered slices are computed.
+function cu_reconst_subvolumes(light_field::CuWavefront{ComplexF32}, transfer_front::CuTransfer{ComplexF32},
+                               transfer_dz::CuTransfer{ComplexF32}, slices::Int, boxes::AbstractVector)
+    n1, n2 = size(light_field.data)
+    @assert size(transfer_front.data) == size(transfer_dz.data) == (n1, n2) "All arrays must have the same size."
+    n = length(boxes)
+    bx = Vector{Int64}(undef, 6n)
+    for (i, b) in enumerate(boxes)
+        bx[6i-5:6i] .= Int64.(collect(b))
+    end
+    offs = zeros(Int64, n + 1)
+    sub(out, wf, tf, td) = _check(ccall((:ph_reconst_subvolumes, libphgb300), Int32,
+                                        (Ptr{Cvoid}, CuPtr{UInt8}, Ptr{Int64}, Ptr{Int64}, Int32, CuPtr{ComplexF32},
+                                         CuPtr{ComplexF32}, CuPtr{ComplexF32}, Int32, Int32, Int32, Ptr{Cvoid}),
+                                        _ctx(), out, offs, bx, n, wf, tf, td, n1, n2, slices, _stream()))
+    sub(CU_NULL, CU_NULL, CU_NULL, CU_NULL)   # sizes only
+    out = CuArray{UInt8}(undef, max(offs[end], 1))
+    n > 0 && sub(out, light_field.data, transfer_front.data, transfer_dz.data)
+    return [reinterpret(N0f8, reshape(out[offs[i]+1:offs[i+1]], b[5] - b[2] + 1, b[4] - b[1] + 1, b[6] - b[3] + 1))
+            for (i, b) in enumerate(boxes)]
+end
+
+# ---- utils.jl ------------------------------------------------------------------------
+
+# Per-pixel mode of the images (the first maximum on ties) / 255, on the host as
+# the reference returns it; images not already UInt8 are scaled by 255 and rounded.
+function cu_make_background_mode(grayimglist)
+    H, W = size(grayimglist[1])
+    imgs = CuArray{UInt8}(undef, H, W, length(grayimglist))
+    for (k, img) in enumerate(grayimglist)
+        u8 = eltype(img) === UInt8 ? img : map(v -> UInt8(round(clamp(Float32(v) * 255f0, 0f0, 255f0))), img)
+        copyto!(view(imgs, :, :, k), u8)
+    end
+    out = CuArray{Float64}(undef, H, W)
+    _check(ccall((:ph_background_mode, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{Float64}, CuPtr{UInt8}, Int64, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), out, imgs, length(grayimglist), H, W, _stream()))
+    return Array(out)
+end
+
+function pad_with_mean(img::CuArray{Float32,2}, padsize::Int)
+    @assert padsize > size(img, 1) && padsize > size(img, 2) "Padsize should be larger than the image size. padsize: $padsize, img size: $(size(img))"
+    out = CuArray{Float32}(undef, padsize, padsize)
+    _check(ccall((:ph_pad_with_mean, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{Float32}, CuPtr{Float32}, Int32, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), out, img, size(img, 1), size(img, 2), padsize, _stream()))
+    return out
+end
+pad_with_mean(img::Array{Float32,2}, padsize::Int) = Array(pad_with_mean(CuArray(img), padsize))
 
 # ---- batches and serving (no single reference counterpart) ------------------------
 
