@@ -269,9 +269,10 @@ def sample_accuracy(ctx, cfg, h1, h2, hp, hpi, hf, hdz, outs, gs_iters, slices, 
     n = cfg["n"]
     dev = h1.device
     wf = torch.empty((n, n), dtype=torch.complex64, device=dev)
+    res = torch.zeros((), dtype=torch.float64, device=dev)
     if gs_iters > 0:
         ctx.call("ph_phase_retrieval", wf.data_ptr(), h1.data_ptr(), h2.data_ptr(), hp.data.data_ptr(),
-                 hpi.data.data_ptr(), n, n, gs_iters, None, s)
+                 hpi.data.data_ptr(), n, n, gs_iters, res.data_ptr(), s)
     else:
         ctx.call("ph_gabor_wavefront", wf.data_ptr(), h1.data_ptr(), n, n, s)
     proj = torch.empty((n, n), dtype=torch.float32, device=dev)
@@ -287,6 +288,8 @@ def sample_accuracy(ctx, cfg, h1, h2, hp, hpi, hf, hdz, outs, gs_iters, slices, 
            "argmin_agreement": float(np.mean(a == outs["arg"])),
            "tolerance": {"rel_l2": 1e-4, "argmin_agreement": 0.999}}
     acc["vs_fp64"] = fp64_accuracy(cfg, h1.cpu().numpy(), h2.cpu().numpy(), w, p, a, gs_iters, slices)
+    if gs_iters > 0:
+        acc["vs_fp64"]["gs_residual"] = float(res.item())   # this path's, FP64-accumulated on the device
     return acc
 
 
@@ -300,18 +303,21 @@ def fp64_accuracy(cfg, h1: np.ndarray, h2: np.ndarray, wf, proj, arg, gs_iters: 
     transfer's square root in FP64): what the FP32 path, with the reference's
     own Float32 transfer arithmetic, gives up against the physics."""
     from oracle import fp64 as o64
+    out = {}
     if gs_iters > 0:
-        wf64 = o64.phase_retrieval_fp64(h1, h2, cfg["gs_sep"], gs_iters, LAM, DX)
+        wf64, out["gs_residual_fp64"] = o64.phase_retrieval_fp64(h1, h2, cfg["gs_sep"], gs_iters, LAM, DX,
+                                                                return_residual=True)
     else:
         wf64 = np.sqrt(np.asarray(h1, dtype=np.float64)).astype(np.complex128)
     p64, a64 = o64.reconst_xyprojection_fp64(wf64, cfg["z0"], cfg["dz"], slices, LAM, DX, with_argmin=True)
     lit = np.abs(wf64) > 0.05   # phases where the field has amplitude
     ph = np.abs(np.exp(1j * np.angle(wf)) - np.exp(1j * np.angle(wf64)))[lit]
-    return {"against": "oracle FP64 (exact physics) on the same sample",
-            "field_rel_l2": rel_l2(wf, wf64),
-            "projection_rel_l2": rel_l2(proj, p64),
-            "argmin_agreement": float(np.mean(arg == a64)),
-            "phase_rms_rad": float(np.sqrt(np.mean(ph ** 2))) if ph.size else 0.0}
+    out.update({"against": "oracle FP64 (exact physics) on the same sample",
+                "field_rel_l2": rel_l2(wf, wf64),
+                "projection_rel_l2": rel_l2(proj, p64),
+                "argmin_agreement": float(np.mean(arg == a64)),
+                "phase_rms_rad": float(np.sqrt(np.mean(ph ** 2))) if ph.size else 0.0})
+    return out
 
 
 def cpu_mvoxel_per_s(cfg, t_it, t_slice, t_ccl) -> float:
