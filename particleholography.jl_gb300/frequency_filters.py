@@ -7,7 +7,6 @@ from __future__ import annotations
 
 import torch
 
-from . import _lib
 from .holofunc import _ctx_stream, _data, _need
 from .types import CuLowPassFilter, CuWavefront
 

@@ -5,7 +5,6 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from . import _lib
 from .holofunc import _ctx_stream, _need
 
 

@@ -2,7 +2,6 @@
 (ccl.jl:13-238) and the reference's known answer (84 components)."""
 import numpy as np
 import pytest
-import torch
 
 from oracle import ccl as occl
 from oracle import ref_semantics as ref

@@ -13,7 +13,7 @@ import pytest
 import torch
 
 from oracle import ref_semantics as ref
-from phtest import ARGMIN_AGREE, REL_L2, rel_l2, to_dev, to_np
+from phtest import ARGMIN_AGREE, REL_L2, rel_l2, to_np
 
 pytestmark = pytest.mark.gpu
 LAM, DX = 0.6328, 10.0
