@@ -81,6 +81,21 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) 
         cfg.numAttrs = 1;
         return cudaLaunchKernelEx(&cfg, kern, body);
     }
+    if constexpr (Body::template pdl<N>()) {
+        // programmatic dependent launch: the grid may start while the previous
+        // kernel on the stream finishes (the body waits before touching its data)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(gx, grid_y);
+        cfg.blockDim = dim3(S::THREADS);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, kern, body);
+    }
     dim3 grid(gx, grid_y);
     kern<<<grid, S::THREADS, smem, s>>>(body);
     return cudaGetLastError();

@@ -86,7 +86,17 @@ struct PassBase {
     // CTAs per thread-block cluster (consecutive blockIdx.x).
     template <int N>
     static constexpr int cluster() { return 1; }
+    // Launched as a programmatic dependent of the previous kernel on the stream
+    // (the body calls grid_dependency_wait before it touches that kernel's data).
+    template <int N>
+    static constexpr bool pdl() { return false; }
 };
+
+// Programmatic dependent launch.  The wait blocks until the kernels this grid
+// depends on have completed and their memory is visible; the trigger lets the
+// next dependent grid be scheduled once every CTA of this one has issued it.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dependents_launch() { asm volatile("griddepcontrol.launch_dependents;" :::); }
 
 constexpr size_t round128(size_t b) { return (b + 127) / 128 * 128; }
 
@@ -844,6 +854,8 @@ struct GsRowMidT : PassBase {
     }
     template <int N>
     static constexpr bool persistent() { return true; }
+    template <int N>
+    static constexpr bool pdl() { return true; }
     template <int N, bool RF>
     static constexpr size_t smem() { return 2 * buf_bytes<N>() + 16; }
 
@@ -872,12 +884,16 @@ struct GsRowMidT : PassBase {
                 bulk_g2s(base + FB + (size_t)q * HS * 4, holo + (size_t)(yb + q) * N, N * 4, bars + buf);
             }
         };
+        // every CTA of this persistent grid is resident: the next pass may be
+        // scheduled onto the SMs this one leaves idle in its last round
+        grid_dependents_launch();
         if (threadIdx.x == 0) {
             mbar_init(bars, 1);
             mbar_init(bars + 1, 1);
             mbar_fence_init();
         }
         __syncthreads();
+        grid_dependency_wait();   // the previous pass wrote src and may still read dst
         if (threadIdx.x == 0 && (int)blockIdx.x < nblocks) issue(blockIdx.x, 0);
         uint32_t parity = 0;
         double acc0 = 0.0, acc1 = 0.0;
@@ -964,6 +980,8 @@ struct GsColT : PassBase {
     }
     template <int N>
     static constexpr bool persistent() { return true; }
+    template <int N>
+    static constexpr bool pdl() { return true; }
     template <int N, bool RF>
     static constexpr size_t smem() {
         return 2 * fbytes<N>() + hbytes<N>() + 32 + tw_extra<N, S<N>::E>(2 * fbytes<N>() + hbytes<N>() + 32);
@@ -1002,6 +1020,7 @@ struct GsColT : PassBase {
             for (int q = 0; q < nv; ++q)
                 bulk_g2s(hbase + (size_t)q * HS * 8, ht + (size_t)(kb + q) * N, N * 8, bars + 2);
         };
+        grid_dependents_launch();   // as in GsRowMidT
         if (threadIdx.x == 0) {
             mbar_init(bars, 1);
             mbar_init(bars + 1, 1);
@@ -1009,10 +1028,11 @@ struct GsColT : PassBase {
             mbar_fence_init();
         }
         __syncthreads();
-        if (threadIdx.x == 0 && (int)blockIdx.x < nblocks) {
-            issue_field(blockIdx.x, 0);
-            issue_ht(blockIdx.x);
-        }
+        // the transfer rows come from an earlier kernel than the one this grid
+        // depends on; the field rows (and the buffer written) only after it
+        if (threadIdx.x == 0 && (int)blockIdx.x < nblocks) issue_ht(blockIdx.x);
+        grid_dependency_wait();
+        if (threadIdx.x == 0 && (int)blockIdx.x < nblocks) issue_field(blockIdx.x, 0);
         uint32_t parity = 0;   // bits 0, 1: field buffers; bit 2: transfer buffer
         int it = 0;
         for (int rb = blockIdx.x; rb < nblocks; rb += gridDim.x, ++it) {
