@@ -50,7 +50,7 @@ CONFIGS = {
                zmin=5000.0, zmax=200000.0, gs_iters=0, gs_sep=0.0, threshold=0.1, seed=3,
                workload="gabor4096_recon1024_ccl"),
     # the 2048^2 frame cut to 64 slices and 2 GS iterations, sized for ncu captures (~3 GB on the
-    # device): GS launches have their c2 size, reconstruction launches a quarter of it (64 of 256 slices)
+    # device): GS launches have their c2 size, reconstruction launches an eighth of it (64 of 512 slices)
     "p2": dict(n=2048, slices=64, dz=200.0, z0=5000.0, discs=800, dmin=10.0, dmax=60.0, zmin=5000.0,
                zmax=100000.0, gs_iters=2, gs_sep=5000.0, threshold=0.1, seed=2,
                workload="gs2048_pr2_recon64_profile"),
@@ -807,7 +807,7 @@ def serve_main(args, cfg, rank, world, local):
         "data": "synthetic (one seeded disc hologram per size, shared by its requests)",
         "config": {"workload": cfg["workload"], "lanes": 3, "capacity_req_s": round(capacity, 2),
                    "saturated_requests": nsat, "form": "fp32-stockham",
-                   "l2": "inputs larger than L2 per request (2048^2 x 512: 8 GiB of slice intermediates)",
+                   "l2": "inputs larger than L2 per request (2048^2 x 512: 16 GiB of slice intermediates, in 2 GiB lane batches)",
                    "parallelism": "single GPU"},
         "p99_frame_ms": p99_09, "serving": rows, "gpu_launches": int(launches), "roofline": None,
         "cpu_baseline": None, "e2e": None, "clocks": clk,
