@@ -671,8 +671,9 @@ int slice_batch(ph_ctx *ctx, int nx, int ny, int slices, size_t target = kBatchB
     if (ctx->opt_slice_batch > 0) return (int)std::min<int64_t>(ctx->opt_slice_batch, slices);
     const size_t slice_bytes = (size_t)nx * ny * sizeof(float2);
     if (ctx->budget) target = std::min(target, ctx->budget / 2);
-    int b = (int)std::max<size_t>(1, target / slice_bytes);
-    return std::min(b, slices);
+    // clamped in size_t: a tiny slice would overflow an int count
+    const size_t b = std::max<size_t>(1, target / slice_bytes);
+    return (int)std::min<size_t>(b, (size_t)std::max(slices, 1));
 }
 
 struct ReconLayout {
