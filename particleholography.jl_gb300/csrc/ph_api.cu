@@ -745,17 +745,25 @@ int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void 
     });
 }
 
-// Slices one pass A / pass B CTA transforms: up to 64 (fewer staging, chain
-// starts and merge steps per slice: 64 measured 1.2 % faster per 2048^2 x 512
-// frame than 32), fewer when the batch would then leave pass A with less than
-// about four CTAs per SM.
-int recon_group(int nbatch, int nx_rows_a) {
+// Slices one pass A / pass B CTA transforms: up to 32, fewer when the batch
+// would then leave pass A with less than about four CTAs per SM.  Where pass A
+// runs the product chain, up to 64 (half the chain starts, each an accurate
+// sin/cos per value) as long as pass A keeps at least 16 waves of CTAs: 1.2 %
+// faster per 2048^2 x 512 frame.  (A 64 cap without the wave condition made
+// 1024^2 x 256 frames 7 % slower: 5 waves, the last one nearly empty.)
+int recon_group(int nbatch, int nx_rows_a, bool chain) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
     const int blocks = std::max(1, nx_rows_a);
     const int groups = std::max(1, (4 * sms + blocks - 1) / blocks);
-    return std::max(1, std::min(64, nbatch / groups));
+    int cap = 32;
+    if (chain) {
+        const int g = std::max(1, std::min(64, nbatch / groups));
+        const long long ctas = (long long)blocks * ((nbatch + g - 1) / g);
+        if (g > 32 && ctas >= 16LL * sms) cap = 64;
+    }
+    return std::max(1, std::min(cap, nbatch / groups));
 }
 
 // The slice loop of a reconstruction: pass A and pass B per batch, then the
@@ -769,7 +777,7 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
     const int row_blocks_a = (nx + recon_a_rows(ny) - 1) / recon_a_rows(ny);
     for (int k0 = first; k0 < first + slices; k0 += L.batch) {
         const int nb = std::min(L.batch, first + slices - k0);
-        const int group = recon_group(nb, row_blocks_a);
+        const int group = recon_group(nb, row_blocks_a, recon_a_chain(ny));
         ReconA a{};
         a.state = state;
         a.t = t;

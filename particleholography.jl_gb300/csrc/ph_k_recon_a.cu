@@ -12,6 +12,15 @@ int recon_a_rows(int n) {
     return 1;
 }
 
+bool recon_a_chain(int n) {
+    switch (n) {
+#define PH_CHAIN_A(N) case N: return ReconA::form<N, true>() == ReconA::FORM_CHAIN;
+        PH_FOR_EACH_N(PH_CHAIN_A)
+#undef PH_CHAIN_A
+    }
+    return false;
+}
+
 cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s) {
     return launch_len<true>(n, b, b.nx, (nbatch + b.group - 1) / b.group, s);
 }
