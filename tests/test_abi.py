@@ -87,3 +87,58 @@ def test_host_mirror_validates_before_launch(ph):
         ph.cu_get_reconst_xyprojection(ph.CuWavefront(a.real.contiguous()), ph.CuTransfer(a), ph.CuTransfer(a), 2)
     with pytest.raises(AssertionError, match="2\\*size"):
         ph.cu_get_reconst_vol_and_xyprojection_padded(ph.CuWavefront(a), ph.CuTransfer(a), ph.CuTransfer(a), 2)
+
+
+def _split_top(s: str) -> list:
+    """Top-level comma split of a parenthesis-free-at-top string."""
+    out, depth, cur = [], 0, ""
+    for ch in s:
+        if ch in "({[":
+            depth += 1
+        elif ch in ")}]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append(cur.strip())
+            cur = ""
+        else:
+            cur += ch
+    if cur.strip():
+        out.append(cur.strip())
+    return out
+
+
+def _close(s: str, i: int) -> int:
+    """Index of the parenthesis closing the one at s[i]."""
+    depth = 0
+    for k in range(i, len(s)):
+        depth += s[k] == "("
+        depth -= s[k] == ")"
+        if depth == 0:
+            return k
+    raise ValueError("unbalanced")
+
+
+def test_julia_ccalls_match_header_arity():
+    """Every ccall of the Julia binding passes as many argument types as the C
+    declaration has parameters (the binding cannot run without Julia)."""
+    hdr = (ROOT / "include" / "phgb300.h").read_text()
+    arity = {}
+    for m in re.finditer(r"\b(ph_[a-z0-9_]+)\s*\(", hdr):
+        start = m.end() - 1
+        params = hdr[start + 1:_close(hdr, start)].strip()
+        if params and params != "void" and not params.startswith("*"):
+            arity[m.group(1)] = len(_split_top(params))
+        elif params in ("", "void"):
+            arity[m.group(1)] = 0
+    jl = (ROOT / "particleholography.jl_gb300" / "julia" / "ParticleHolographyGB300.jl").read_text()
+    checked = 0
+    for m in re.finditer(r"ccall\(\(:(ph_[a-z0-9_]+), libphgb300\),", jl):
+        name = m.group(1)
+        rest = jl[m.end():]
+        ret = _split_top(rest[:rest.index("(")] + "x")[0]   # the return type, up to the type tuple
+        i = rest.index("(")
+        types = _split_top(rest[i + 1:_close(rest, i)])
+        assert name in arity, name
+        assert len(types) == arity[name], (name, len(types), arity[name], ret)
+        checked += 1
+    assert checked >= 20
