@@ -122,13 +122,16 @@ def test_julia_ccalls_match_header_arity():
     """Every ccall of the Julia binding passes as many argument types as the C
     declaration has parameters (the binding cannot run without Julia)."""
     hdr = (ROOT / "include" / "phgb300.h").read_text()
-    arity = {}
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)   # declarations only
+    arity, c_params = {}, {}
     for m in re.finditer(r"\b(ph_[a-z0-9_]+)\s*\(", hdr):
         start = m.end() - 1
         params = hdr[start + 1:_close(hdr, start)].strip()
         if params and params != "void" and not params.startswith("*"):
-            arity[m.group(1)] = len(_split_top(params))
+            c_params[m.group(1)] = _split_top(params)
+            arity[m.group(1)] = len(c_params[m.group(1)])
         elif params in ("", "void"):
+            c_params[m.group(1)] = []
             arity[m.group(1)] = 0
     jl = (ROOT / "particleholography.jl_gb300" / "julia" / "ParticleHolographyGB300.jl").read_text()
     checked = 0
@@ -140,5 +143,24 @@ def test_julia_ccalls_match_header_arity():
         types = _split_top(rest[i + 1:_close(rest, i)])
         assert name in arity, name
         assert len(types) == arity[name], (name, len(types), arity[name], ret)
+        for jt, ct in zip(types, c_params[name]):
+            assert _kind_jl(jt) == _kind_c(ct), (name, jt, ct)
         checked += 1
     assert checked >= 20
+
+
+def _kind_c(param: str) -> str:
+    p = param.replace("const ", "").strip()
+    if "*" in p:
+        return "ptr"
+    t = p.split()[0]
+    return {"int32_t": "i32", "int64_t": "i64", "double": "f64", "float": "f32", "size_t": "size",
+            "uint32_t": "u32"}.get(t, t)
+
+
+def _kind_jl(t: str) -> str:
+    t = t.strip()
+    if t.startswith(("Ptr{", "CuPtr{", "Ref{", "Cstring")):
+        return "ptr"
+    return {"Int32": "i32", "Int64": "i64", "Float64": "f64", "Float32": "f32", "Csize_t": "size",
+            "UInt32": "u32"}.get(t, t)
