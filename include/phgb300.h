@@ -174,6 +174,27 @@ PH_API int32_t ph_reconst_xyproj(ph_ctx *ctx, float *proj, int32_t *argmin, cons
                           const void *tf_front, const void *tf_dz,
                           int32_t n_fast, int32_t n_slow, int32_t slices, void *stream);
 
+/* One depth shard of cu_get_reconst_xyprojection (holofunc.jl:248-266; its
+ * serial slice loop :259-263): slices k in [k0, k1) with their GLOBAL index,
+ * X_k = fftshift(fft(wf)).*tf_front.*tf_dz^k, reduced to packed words
+ * packed[y][x] = (float bits of min_k |slice_k|^2) << 32 | k, first minimum on
+ * ties.  accumulate = 0 first fills packed with PH_PACKED_EMPTY; 1 merges into
+ * the words already there (a min per word).  Shards of one frame merged by a
+ * per-word minimum (this call with accumulate = 1, or an int64 MIN all-reduce
+ * across GPUs: every word, and the identity, is a non-negative int64) give the
+ * projection and argmin of one ph_reconst_xyproj over [0, S); unpack them
+ * with ph_unpack_projection.  k1 == k0 contributes the identity. */
+#define PH_PACKED_EMPTY 0x7fffffffffffffffLL
+PH_API int32_t ph_reconst_xyproj_range(ph_ctx *ctx, int64_t *packed, const void *wf, const void *tf_front,
+                                       const void *tf_dz, int32_t n_fast, int32_t n_slow, int32_t k0, int32_t k1,
+                                       int32_t accumulate, void *stream);
+
+/* Packed words -> projection (float bits, nullable) and argmin (slice, nullable):
+ * the proj that cu_get_reconst_xyprojection returns (holofunc.jl:265), from
+ * the merged shards of ph_reconst_xyproj_range. */
+PH_API int32_t ph_unpack_projection(ph_ctx *ctx, float *proj, int32_t *argmin, const int64_t *packed,
+                                    int32_t n_fast, int32_t n_slow, void *stream);
+
 /* cu_apply_low_pass_filter (frequency_filters.jl:88-107) followed by
  * cu_get_reconst_xyprojection (holofunc.jl:248-266), with the filter folded
  * into the spectrum: X_k = fftshift(fft(wf)) .* lpf .* tf_front .* tf_dz^k, no

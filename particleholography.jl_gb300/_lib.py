@@ -32,6 +32,9 @@ PH_OPT_USE_GRAPHS = 2
 PH_OPT_LOOP_LIMIT = 3
 PH_OPT_PROFILE = 4
 
+# identity of the packed-minimum merge (ph_reconst_xyproj_range)
+PH_PACKED_EMPTY = 0x7FFFFFFFFFFFFFFF
+
 _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64
@@ -58,6 +61,8 @@ SIGNATURES = {
     "ph_phase_retrieval": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp]),
     "ph_asm_prop": (_i32, [_vp, _vp, _vp, _vp, _f64, _i32, _i32, _f64, _vp]),
     "ph_reconst_xyproj": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
+    "ph_reconst_xyproj_range": (_i32, [_vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
+    "ph_unpack_projection": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _vp]),
     "ph_reconst_xyproj_lpf": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "ph_reconst_binary_vol": (_i32, [_vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "ph_reconst_subvolumes": (_i32, [_vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),

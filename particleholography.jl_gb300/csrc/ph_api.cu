@@ -287,6 +287,17 @@ __global__ void k_proj_finish(const unsigned long long *p64, float *proj, int32_
     if (argmin) argmin[i] = (int32_t)(unsigned)(p & 0xffffffffu);
 }
 
+// The identity of the packed-minimum merge: INT64_MAX (float bits 0x7fffffff,
+// slice 0xffffffff).  Every packed word of a finite or NaN intensity orders
+// below it, unsigned and signed alike (a non-negative float's sign bit is 0),
+// so shards merged by any backend's int64 MIN never pick it over a real word.
+constexpr unsigned long long kPackedEmpty = 0x7fffffffffffffffull;
+
+__global__ void k_fill_u64(unsigned long long *p, size_t n, unsigned long long v) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
 __global__ void k_binarize_le(uint8_t *out, const float *in, size_t n, float thr) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = in[i] <= thr ? 1 : 0;
@@ -711,9 +722,15 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
                        cudaStream_t s, float threshold = 0.0f, int first = 0, const SubArgs *sub = nullptr);
 
 // Shared driver of every reconstruction entry point.
+//
+// With `packed` (RK_PROJ only) the minimum of slices [first, first + slices)
+// is merged into the caller's packed words (float bits << 32 | global slice)
+// instead of the context's scratch, which `accumulate` = false first fills with
+// the merge identity; no projection is unpacked.
 int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype,
                 const float2 *wf, const float2 *hf, const float2 *hdz, int nin_x, int nin_y, int slices,
-                cudaStream_t s, const float *lpf = nullptr, float threshold = 0.0f) {
+                cudaStream_t s, const float *lpf = nullptr, float threshold = 0.0f,
+                unsigned long long *packed = nullptr, bool accumulate = false, int first = 0) {
     const bool padded = kind == RK_PADDED;
     const int nx = padded ? 2 * nin_x : nin_x;
     const int ny = padded ? 2 * nin_y : nin_y;
@@ -727,21 +744,32 @@ int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void 
     PH_TRY(get_twiddles(ctx, nx, s, &tw_x));
     PH_TRY(get_twiddles(ctx, ny, s, &tw_y));
     float4 *state = at<float4>(ctx, L.state);
-    auto *p64 = at<unsigned long long>(ctx, L.p64);
+    auto *p64 = packed != nullptr ? packed : at<unsigned long long>(ctx, L.p64);
     float2 *t = at<float2>(ctx, L.t);
     const bool want_proj = (kind == RK_PROJ) || proj != nullptr || argmin != nullptr;
     char key[512];
     uint32_t thr_bits = 0;
     memcpy(&thr_bits, &threshold, sizeof thr_bits);
-    snprintf(key, sizeof key, "recon|%d|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%d|%p|%08x", (int)kind, nin_x, nin_y,
-             slices, L.batch, vol_dtype, (void *)proj, (void *)argmin, vol, (const void *)wf, (const void *)hf,
-             (const void *)hdz, ctx->scratch, (int)ctx->opt_loop_limit, (const void *)lpf, thr_bits);
+    snprintf(key, sizeof key, "recon|%d|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%d|%p|%08x|%p|%d|%d", (int)kind, nin_x,
+             nin_y, slices, L.batch, vol_dtype, (void *)proj, (void *)argmin, vol, (const void *)wf, (const void *)hf,
+             (const void *)hdz, ctx->scratch, (int)ctx->opt_loop_limit, (const void *)lpf, thr_bits, (void *)packed,
+             (int)accumulate, first);
     return run_graph(ctx, s, key, [&](cudaStream_t s) -> int {
         PH_TRY(issue_spectrum(ctx, wf, hf, hdz, nx, ny, padded, nin_x, nin_y, at<float2>(ctx, L.a1), state, tw_x,
                               tw_y, at<double>(ctx, L.acc), at<float2>(ctx, L.mean), s, nullptr, lpf));
-        if (want_proj) PH_CUDA(cudaMemsetAsync(p64, 0xff, sizeof(unsigned long long) * nx_out * ny_out, s), "memset");
+        const size_t npix = (size_t)nx_out * ny_out;
+        if (packed != nullptr) {
+            if (!accumulate) {
+                k_fill_u64<<<(unsigned)std::min<size_t>((npix + 255) / 256, 4096), 256, 0, s>>>(p64, npix,
+                                                                                               kPackedEmpty);
+                PH_TRY(launched(ctx, cudaGetLastError(), "packed fill"));
+            }
+        } else if (want_proj) {
+            PH_CUDA(cudaMemsetAsync(p64, 0xff, sizeof(unsigned long long) * npix, s), "memset");
+        }
         return issue_recon_slices(ctx, kind, proj, argmin, vol, vol_dtype, nx, ny, nx_out, ny_out, x0, y0, slices,
-                                  L.batch, state, t, p64, tw_x, tw_y, want_proj, s, threshold);
+                                  L.batch, state, t, p64, tw_x, tw_y, want_proj && packed == nullptr, s, threshold,
+                                  first);
     });
 }
 
@@ -819,7 +847,7 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
             PH_TRY(pass(ctx, s, "recon_b",[&] { return launch_recon_b(nx, b, s); }));
         }
     }
-    if (want_proj) {
+    if (want_proj && (proj != nullptr || argmin != nullptr)) {
         const size_t n = (size_t)nx_out * ny_out;
         k_proj_finish<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p64, proj, argmin, n);
         PH_TRY(launched(ctx, cudaGetLastError(), "projection finish"));
@@ -1392,6 +1420,45 @@ int32_t ph_reconst_xyproj(ph_ctx *ctx, float *proj, int32_t *argmin, const void 
     PH_TRY(reconstruct(ctx, RK_PROJ, proj, argmin, nullptr, PH_F32, static_cast<const float2 *>(wf),
                        static_cast<const float2 *>(tf_front), static_cast<const float2 *>(tf_dz), n_fast, n_slow,
                        slices, s));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_reconst_xyproj_range(ph_ctx *ctx, int64_t *packed, const void *wf, const void *tf_front,
+                                const void *tf_dz, int32_t n_fast, int32_t n_slow, int32_t k0, int32_t k1,
+                                int32_t accumulate, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(packed, "packed");
+    PH_NONNULL(wf, "wavefront");
+    PH_NONNULL(tf_front, "transfer_front");
+    PH_NONNULL(tf_dz, "transfer_dz");
+    if (k0 < 0 || k1 < k0) { set_err(ctx, "slice range [%d, %d) is invalid", k0, k1); return PH_ERR_SIZE; }
+    auto *p = reinterpret_cast<unsigned long long *>(packed);
+    if (k1 == k0) {
+        // an empty shard contributes the merge identity
+        PH_TRY(check_len(ctx, n_fast, n_slow));
+        if (!accumulate) {
+            const size_t npix = (size_t)n_fast * n_slow;
+            k_fill_u64<<<(unsigned)std::min<size_t>((npix + 255) / 256, 4096), 256, 0, s>>>(p, npix, kPackedEmpty);
+            PH_TRY(launched(ctx, cudaGetLastError(), "packed fill"));
+        }
+        PH_LEAVE(ctx);
+    }
+    PH_TRY(reconstruct(ctx, RK_PROJ, nullptr, nullptr, nullptr, PH_F32, static_cast<const float2 *>(wf),
+                       static_cast<const float2 *>(tf_front), static_cast<const float2 *>(tf_dz), n_fast, n_slow,
+                       k1 - k0, s, nullptr, 0.0f, p, accumulate != 0, k0));
+    PH_LEAVE(ctx);
+}
+
+int32_t ph_unpack_projection(ph_ctx *ctx, float *proj, int32_t *argmin, const int64_t *packed, int32_t n_fast,
+                             int32_t n_slow, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_NONNULL(packed, "packed");
+    if (proj == nullptr && argmin == nullptr) { set_err(ctx, "proj and argmin are both NULL"); return PH_ERR_INVALID; }
+    if (n_fast < 1 || n_slow < 1) { set_err(ctx, "size %d x %d is invalid", n_fast, n_slow); return PH_ERR_SIZE; }
+    const size_t n = (size_t)n_fast * n_slow;
+    k_proj_finish<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(reinterpret_cast<const unsigned long long *>(packed),
+                                                                proj, argmin, n);
+    PH_TRY(launched(ctx, cudaGetLastError(), "projection unpack"));
     PH_LEAVE(ctx);
 }
 

@@ -210,16 +210,19 @@ __device__ __forceinline__ uint32_t phase_turns_u32(float2 h, const double2 *__r
     return ((uint32_t)i << 20) + (uint32_t)__float2int_rn(phi * (4294967296.0f / 6.28318530717958647692f));
 }
 
-// |h| - 1: (|h|^2 - 1) in FP64 from exact products (no cancellation error
-// near |h| = 1), over |h| + 1 in FP32.
-__device__ __forceinline__ float modulus_minus_one(float2 h) {
+// log2 |h|.  |h| - 1 comes from (|h|^2 - 1) in FP64 from exact products (no
+// cancellation error near |h| = 1) over |h| + 1 in FP32, then log1pf.  h = 0
+// gives -1e30 rather than -inf, so that k log2|h| is 0 at k = 0 (|h|^0 = 1)
+// and |h|^k underflows to 0 for every k >= 1.
+__device__ __forceinline__ float log2_modulus(float2 h) {
     const double v = (double)h.x * h.x + (double)h.y * h.y - 1.0;
-    return (float)v / (sqrtf(fmaf(h.x, h.x, h.y * h.y)) + 1.0f);
+    const float w = (float)v / (sqrtf(fmaf(h.x, h.x, h.y * h.y)) + 1.0f);
+    return fmaxf(log1pf(w) * 1.44269504088896340736f, -1e30f);
 }
 
 // Rows kx of the forward-row output, FFT along y, times the front transfer
 // (and 1/(nx ny)), stored with the slice phase rate of the slice transfer:
-// state[kx][ky] = (X0, turns(Hdz), |Hdz| - 1).
+// state[kx][ky] = (X0, turns(Hdz), log2 |Hdz|).
 struct SpectrumCols : PassBase {
     const float2 *a1;        // [nx][ny]
     const float2 *hf, *hdz;  // centred [ny][nx]
@@ -245,7 +248,7 @@ struct SpectrumCols : PassBase {
                 const float2 x0 = cscale(cmul(v, hf[c]), lpf != nullptr ? scale * lpf[c] : scale);
                 const float2 d = hdz[c];
                 state[(size_t)kx * N + ky] =
-                    make_float4(x0.x, x0.y, __uint_as_float(phase_turns_u32(d, ptab)), modulus_minus_one(d));
+                    make_float4(x0.x, x0.y, __uint_as_float(phase_turns_u32(d, ptab)), log2_modulus(d));
             });
     }
 };
@@ -255,7 +258,7 @@ struct SpectrumCols : PassBase {
 // Slice k of rows kx: X_k = X0 * Hdz^k; inverse FFT along ky; transposed store
 // T[b][y - y0][kx] for y in [y0, y0 + ny_out).  Hdz^k X0 evaluated directly
 // from the state uses the phase rate times k in exact integer turn arithmetic
-// and |Hdz|^k ~ 1 + k (|Hdz| - 1).
+// and |Hdz|^k = 2^(k log2 |Hdz|).
 //
 // A CTA transforms `group` consecutive slices from rows staged in shared
 // memory once (the staging forms are described at FORM_CHAIN .. FORM_NONE).
@@ -293,7 +296,7 @@ struct ReconA : PassBase {
     //  FORM_STATE: the state rows, staged by bulk copy; every slice evaluates
     //    Hdz^k from them.
     //  FORM_X0: only X0 (8 of the state's 16 bytes) staged; the phase rate
-    //    and |Hdz| - 1 come from L2 every slice.  (3 * 2^a lengths, whose
+    //    and log2 |Hdz| come from L2 every slice.  (3 * 2^a lengths, whose
     //    24-value threads give a CTA 8 rows: their full state does not fit.)
     //  FORM_NONE: the whole state from L2 every slice.
     // The chain saves the per-voxel sin/cos; the direct forms move fewer
@@ -346,13 +349,15 @@ struct ReconA : PassBase {
     static constexpr size_t smem() {
         return stage_total<N, RF>() + Shape<N, EPT, TT>::template smem_bytes<RF>();
     }
-    // Hdz^k X0 from the state (re, im, phase-rate bits, |Hdz| - 1).
+    // Hdz^k X0 from the state (re, im, phase-rate bits, log2 |Hdz|): the phase
+    // k p in exact integer turn arithmetic, the modulus |Hdz|^k = 2^(k log2|Hdz|)
+    // (exact for any transfer, unit or not).
     __device__ __forceinline__ static float2 direct(const float4 s, uint32_t k) {
         const int32_t tt = (int32_t)(k * __float_as_uint(s.z));
         const float ang = (float)tt * 1.46291807926715968e-9f;   // 2 pi / 2^32
         float sn, cs;
         __sincosf(ang, &sn, &cs);
-        const float mag = fmaf((float)k, s.w, 1.0f);
+        const float mag = exp2f((float)k * s.w);
         return cmul(make_float2(s.x, s.y), make_float2(cs * mag, sn * mag));
     }
 
@@ -390,7 +395,7 @@ struct ReconA : PassBase {
                     // Hdz itself: the accurate sin/cos, as its error grows along the chain
                     float sn, cs;
                     sincospif((float)(int32_t)__float_as_uint(st.z) * 4.656612873077392578125e-10f, &sn, &cs);
-                    const float mag = 1.0f + st.w;
+                    const float mag = exp2f(st.w);
                     h = make_float2(cs * mag, sn * mag);
                 }
                 xs[col] = x;

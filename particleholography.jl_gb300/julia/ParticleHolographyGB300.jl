@@ -18,7 +18,8 @@ export cu_transfer_sqrt_arr, cu_transfer, cu_gabor_wavefront, cu_phase_retrieval
        cu_get_reconst_xyprojection, cu_get_reconst_vol_and_xyprojection, cu_get_reconst_complex_vol,
        cu_asm_prop!, cu_2d_pad, cu_get_reconst_vol_and_xyprojection_padded,
        cu_connected_component_labeling, count_labels, cu_find_valid_labels,
-       cu_get_reconst_xyprojection_argmin, cu_apply_low_pass_filter!, cu_apply_low_pass_filter,
+       cu_get_reconst_xyprojection_argmin, cu_get_reconst_xyprojection_range, unpack_projection,
+       cu_apply_low_pass_filter!, cu_apply_low_pass_filter,
        cu_rectangle_filter, cu_super_gaussian_filter, cu_get_reconst_xyprojection_lpf,
        cu_get_reconst_binary_vol, slice_bounding_rectangles, cu_reconst_subvolumes,
        cu_make_background_mode, pad_with_mean,
@@ -149,6 +150,33 @@ function cu_get_reconst_xyprojection_argmin(wavefront::CuWavefront{ComplexF32}, 
                                             transfer_dz::CuTransfer{ComplexF32}, slices::Int)
     arg = CuArray{Int32}(undef, size(wavefront.data)...)
     proj = _xyproj(wavefront, transfer_front, transfer_dz, slices, arg)
+    return proj, arg .+ Int32(1)
+end
+
+"""New: one depth shard of `cu_get_reconst_xyprojection`, slices `k0:k1-1`
+(0-based, global) reduced to packed words `(Float32 bits << 32) | slice`.
+Merge the shards of a frame with `min.` (or an `Int64` MIN all-reduce across
+GPUs) and unpack them with `unpack_projection`."""
+function cu_get_reconst_xyprojection_range(wavefront::CuWavefront{ComplexF32}, transfer_front::CuTransfer{ComplexF32},
+                                           transfer_dz::CuTransfer{ComplexF32}, k0::Int, k1::Int;
+                                           packed::Union{CuArray{Int64,2},Nothing}=nothing, accumulate::Bool=false)
+    @assert size(wavefront.data) == size(transfer_front.data) == size(transfer_dz.data) "All arrays must have the same size. Got $(size(wavefront.data)), $(size(transfer_front.data)), $(size(transfer_dz.data))."
+    out = packed === nothing ? CuArray{Int64}(undef, size(wavefront.data)...) : packed
+    _check(ccall((:ph_reconst_xyproj_range, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{Int64}, CuPtr{ComplexF32}, CuPtr{ComplexF32}, CuPtr{ComplexF32},
+                  Int32, Int32, Int32, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), out, wavefront.data, transfer_front.data, transfer_dz.data, size(wavefront.data, 1),
+                 size(wavefront.data, 2), k0, k1, accumulate ? Int32(1) : Int32(0), _stream()))
+    return out
+end
+
+"New: merged packed words -> (projection, 1-based slice index of the first minimum)."
+function unpack_projection(packed::CuArray{Int64,2})
+    proj = CuArray{Float32}(undef, size(packed)...)
+    arg = CuArray{Int32}(undef, size(packed)...)
+    _check(ccall((:ph_unpack_projection, libphgb300), Int32,
+                 (Ptr{Cvoid}, CuPtr{Float32}, CuPtr{Int32}, CuPtr{Int64}, Int32, Int32, Ptr{Cvoid}),
+                 _ctx(), proj, arg, packed, size(packed, 1), size(packed, 2), _stream()))
     return proj, arg .+ Int32(1)
 end
 

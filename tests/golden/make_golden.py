@@ -13,7 +13,7 @@ All arrays are stored in the C order of the Julia buffer: a Julia array of size
 ``(n_fast, n_slow)`` is a numpy array of shape ``(n_slow, n_fast)``; an image
 as displayed (row, col) is therefore stored transposed.
 
-Usage: ``python tests/golden/make_golden.py [path-to-reference-checkout]``.
+Usage: ``python tests/golden/make_golden.py <path-to-reference-checkout>``.
 """
 from __future__ import annotations
 
@@ -195,11 +195,13 @@ def oracle_vectors():
 
 
 if __name__ == "__main__":
-    refroot = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
-    if (refroot / "test" / "data").exists():
-        reference_data(refroot)
-    else:
-        print(f"no reference checkout at {refroot}: keeping the committed reference-data fixtures")
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0] if __doc__ else None)
+    ap.add_argument("reference", type=Path, help="checkout of ParticleHolography.jl (its test/data fixtures)")
+    refroot = ap.parse_args().reference
+    if not (refroot / "test" / "data").exists():
+        sys.exit(f"{refroot} holds no test/data: give the path of a ParticleHolography.jl checkout")
+    reference_data(refroot)
     oracle_vectors()
     for f in sorted(HERE.glob("*.npz")):
         print(f"{f.name}: {f.stat().st_size} bytes")

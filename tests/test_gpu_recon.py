@@ -175,3 +175,34 @@ def test_long_slice_groups(ph, cuda):
         assert rel_l2(p, p_ref) < REL_L2
         assert np.mean(a == a_ref) >= ARGMIN_AGREE
         assert rel_l2(p, outs[0][0]) < 1e-5
+
+
+# Non-unit slice transfers: |Hdz|^k must be exact, not 1 + k(|Hdz| - 1).  Each
+# length exercises one pass A form: 512 / 2048 the product chain, 256 / 1024
+# the staged state, 1536 the staged X0 with the phase rate from L2, 4096 the
+# cluster store.
+@pytest.mark.parametrize("n,slices,mag", [(256, 512, 0.999), (512, 512, 0.999), (1024, 96, 1.001),
+                                          (1536, 64, 0.99), (2048, 64, 0.99), (4096, 16, 0.95)])
+def test_non_unit_slice_transfer(ph, cuda, n, slices, mag):
+    holo, hf, hdz = _case(n, seed=n + 1, dz=-150.0)
+    hdz = (hdz * np.float32(mag)).astype(np.complex64)
+    wf = ph.cu_gabor_wavefront(to_dev(holo, cuda))
+    proj, arg = ph.cu_get_reconst_xyprojection(wf, ph.CuTransfer(to_dev(hf, cuda)), ph.CuTransfer(to_dev(hdz, cuda)),
+                                               slices, return_argmin=True)
+    p_ref, a_ref = ref.reconst_xyprojection(ref.gabor_wavefront(holo), hf, hdz, slices, with_argmin=True)
+    assert rel_l2(to_np(proj), p_ref) < REL_L2
+    assert np.mean(to_np(arg) == a_ref) >= ARGMIN_AGREE
+
+
+def test_non_unit_complex_slices(ph, cuda):
+    """Every slice of the complex volume with |Hdz| = 0.99 over 64 slices (0.53
+    at the last one) against the oracle's cumulative product."""
+    n, slices = 512, 64
+    holo, hf, hdz = _case(n, seed=21, dz=-150.0)
+    hdz = (hdz * np.float32(0.99)).astype(np.complex64)
+    wf = ph.cu_gabor_wavefront(to_dev(holo, cuda))
+    cv = to_np(ph.cu_get_reconst_complex_vol(wf, ph.CuTransfer(to_dev(hf, cuda)), ph.CuTransfer(to_dev(hdz, cuda)),
+                                             slices))
+    cv_ref = ref.reconst_complex_vol(ref.gabor_wavefront(holo), hf, hdz, slices)
+    for k in range(slices):
+        assert rel_l2(cv[k], cv_ref[k]) < REL_L2, k

@@ -129,3 +129,20 @@ def test_pack_orders_like_values(ph):
     assert order.tolist() == [0, 1, 3, 2, 4, 5]
     p, a = parallel.unpack(packed)
     assert torch.equal(p, v) and torch.equal(a, k)
+
+
+def test_packed_identity_matches_library_header():
+    """The merge identity the gloo ranks use is the library's PH_PACKED_EMPTY, so
+    shards produced by ph_reconst_xyproj_range merge with these words as is."""
+    import re
+    import __graft_entry__ as g
+    g.load_package()
+    from ph_gb300 import _lib, parallel
+    hdr = (g.ROOT / "include" / "phgb300.h").read_text()
+    m = re.search(r"#define PH_PACKED_EMPTY (0x[0-9a-fA-F]+)LL", hdr)
+    assert m is not None
+    assert int(m.group(1), 16) == _lib.PH_PACKED_EMPTY == parallel.PACKED_EMPTY == np.iinfo(np.int64).max
+    # every packed word of a non-negative float (finite, inf or NaN) orders below it, signed and unsigned
+    for f in (0.0, 1e-30, 1.0, 3.4e38, float("inf"), float("nan")):
+        w = parallel.pack(torch.tensor([f], dtype=torch.float32), torch.tensor([0x7FFFFFFF], dtype=torch.int32))
+        assert int(w[0]) < parallel.PACKED_EMPTY
