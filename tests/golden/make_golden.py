@@ -125,6 +125,23 @@ def reference_data(refroot: Path):
     h2 = gray_u8(read_png(data / "holo2_corrected.png")).T
     c = slice(384, 640)
     np.savez_compressed(HERE / "holo_crops.npz", holo1=h1[c, c].copy(), holo2=h2[c, c].copy())
+    pipeline_data(refroot)
+
+
+def pipeline_data(refroot: Path):
+    """Inputs and output of the reference's end-to-end detection test
+    (``test/runtests.jl:153-193``): the full 1024^2 holograms ``holo1.bmp`` /
+    ``holo2.bmp`` as 8-bit levels in Julia buffer order, and the 22 particle
+    coordinates ``[x, y, z_slice]`` the reference wrote to
+    ``test/data/particles.json`` (UUID keys dropped: they are time-based)."""
+    import json
+    data = refroot / "test" / "data"
+    h1 = gray_u8(read_bmp(data / "holo1.bmp")).T.copy()
+    h2 = gray_u8(read_bmp(data / "holo2.bmp")).T.copy()
+    coords = json.loads((data / "particles.json").read_text())
+    rows = np.array(sorted(coords.values()), dtype=np.float32).reshape(-1, 3)
+    np.savez_compressed(HERE / "holo_pair.npz", holo1=h1, holo2=h2)
+    np.savez_compressed(HERE / "particles_ref.npz", coords=rows)
 
 
 def oracle_vectors():

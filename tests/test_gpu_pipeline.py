@@ -1,0 +1,76 @@
+"""The library pinned to the reference's own output: the reference's end-to-end
+detection test (test/runtests.jl:153-193) through libphgb300 -- phase
+retrieval, the N0f8 volume, threshold, per-slice labeling and boxes on the
+device, the sub-volumes particle_coordinates cuts out -- against the 22
+particles of test/data/particles.json and against the oracle's volume.
+
+The neighbourhood bookkeeping between slices (ccl.jl:266-467) is host logic
+the reference keeps in Julia dictionaries; here the oracle's restatement of it
+runs on the library's per-slice boxes."""
+import numpy as np
+import pytest
+import torch
+
+import pipeline_case as pc
+from oracle import detect_ref as dr
+from oracle import ref_semantics as ref
+from phtest import to_dev, to_np
+
+pytestmark = pytest.mark.gpu
+
+# The library's FFT is not cuFFT: N0f8 levels may flip where an intensity lies
+# within rounding of a level boundary, which can move a box edge by a pixel and
+# a centre of mass by a fraction of one.
+TOL_XY = 0.5      # pixels
+TOL_Z = 2.0       # slices
+
+
+@pytest.fixture(scope="module")
+def library_run(ph, cuda):
+    h1, h2 = pc.holograms()
+    n = pc.DATLEN
+    d = ph.cu_transfer_sqrt_arr(n, pc.LAM, pc.DX)
+    u = ph.cu_phase_retrieval_holo(to_dev(h1, cuda), to_dev(h2, cuda), ph.cu_transfer(pc.PR_DIST, n, pc.LAM, d),
+                                   ph.cu_transfer(-pc.PR_DIST, n, pc.LAM, d), pc.PR_ITER, n)
+    tf, ts = ph.cu_transfer(-pc.Z0, n, pc.LAM, d), ph.cu_transfer(-pc.DZ, n, pc.LAM, d)
+    vol = ph.cu_get_reconst_vol(u, tf, ts, pc.SLICES)                       # N0f8 levels, (S, n, n)
+    rects = ph.slice_bounding_boxes(vol <= pc.THRESHOLD_LEVEL)
+    boxes = dr.neighborhoods_from_rectangles([[tuple(r[1:]) for r in sl.tolist()] for sl in rects])
+    subs = ph.cu_reconst_subvolumes(u, tf, ts, pc.SLICES, boxes)
+    coords = ph.particle_coordinates(np.array(boxes), subs)
+    return {"u": u, "vol": to_np(vol), "boxes": boxes, "coords": coords, "subs": [to_np(s) for s in subs]}
+
+
+def test_library_reproduces_reference_particles(library_run):
+    got, want = library_run["coords"], pc.reference_particles()
+    pairs, extra, missing = dr.match_particles(got, want, TOL_XY, TOL_Z)
+    dev = np.array([np.abs(got[i] - want[j]) for i, j in pairs])
+    print(f"{len(pairs)} of {len(want)} matched; max |dx|,|dy| {dev[:, :2].max():.4f} px, max |dz| {dev[:, 2].max():.0f}; "
+          f"exact (1e-3 px, same slice): {int(np.sum((dev[:, :2].max(axis=1) < 1e-3) & (dev[:, 2] == 0)))}")
+    assert not extra and not missing, (got[extra], want[missing])
+    assert len(pairs) == 22
+
+
+def test_library_volume_matches_oracle_volume(library_run):
+    """The whole 1024^2 x 1000 N0f8 volume against the oracle's: levels differ
+    by at most one, and only where the FP32 intensity sits at a level boundary."""
+    h1, h2 = pc.holograms()
+    n = pc.DATLEN
+    d = ref.transfer_sqrt_arr(n, pc.LAM, pc.DX)
+    u = ref.phase_retrieval_holo(h1, h2, ref.transfer(pc.PR_DIST, n, pc.LAM, d),
+                                 ref.transfer(-pc.PR_DIST, n, pc.LAM, d), pc.PR_ITER, n)
+    vol = library_run["vol"]
+    flips = 0
+    for k, x in enumerate(ref.iter_slices(u, ref.transfer(-pc.Z0, n, pc.LAM, d), ref.transfer(-pc.DZ, n, pc.LAM, d),
+                                          pc.SLICES)):
+        diff = np.abs(vol[k].astype(np.int16) - ref.ifft_and_abs(x, ref.N0f8).astype(np.int16))
+        assert diff.max() <= 1, k
+        flips += int(np.count_nonzero(diff))
+    assert flips / vol.size < 1e-4, flips
+
+
+def test_subvolumes_equal_volume_crops(library_run):
+    """The sub-volumes computed without the volume equal crops of the volume."""
+    vol = library_run["vol"]
+    for (x0, y0, z0, x1, y1, z1), sv in zip(library_run["boxes"], library_run["subs"]):
+        assert np.array_equal(sv, vol[z0 - 1:z1, x0 - 1:x1, y0 - 1:y1])
