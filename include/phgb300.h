@@ -72,8 +72,32 @@ enum {
     PH_OPT_SLICE_BATCH = 1,   /* slices per reconstruction batch (0 = automatic) */
     PH_OPT_USE_GRAPHS = 2,    /* 1 = replay cached CUDA graphs for repeated shapes (default 1) */
     PH_OPT_LOOP_LIMIT = 3,    /* iteration limit of bounded device loops (CCL root chase) */
-    PH_OPT_PROFILE = 4        /* 1 = time every pass kernel with CUDA events (ph_profile_report) */
+    PH_OPT_PROFILE = 4,       /* 1 = time every pass kernel with CUDA events (ph_profile_report) */
+    PH_OPT_FORM = 5           /* arithmetic of the projection's row pass: PH_FORM_* (default FP32) */
 };
+
+/* forms of the projection's row pass (ph_reconst_xyproj and its range and
+ * batch forms, row lengths 1024 and 2048; other lengths and the volume paths
+ * stay FP32).  The split forms run the row DFT as two complex DFT GEMMs on the
+ * tensor cores with FP32 accumulation, each operand held as a hi + lo pair of
+ * 16-bit words: */
+enum {
+    PH_FORM_FP32 = 0,     /* radix-16 Stockham FFT on the CUDA cores, FP32 */
+    PH_FORM_BF16X3 = 1,   /* BF16 pairs, products hi.hi + lo.hi + hi.lo */
+    PH_FORM_FP16X3 = 2,   /* FP16 pairs (tiles scaled by powers of two), three products */
+    PH_FORM_FP16X2 = 3    /* FP16 data pairs, DFT matrix in one FP16 word: hi.hi + lo.hi */
+};
+
+/* ---- diagnostics ----------------------------------------------------------- */
+
+/* Tensor-core self-test, no counterpart in the reference: d[128][n] (FP32) =
+ * a[128][k] . b[n][k]^T for BF16 (fp16 = 0) or FP16 (fp16 = 1) operand bits,
+ * computed by one tcgen05 MMA chain with the operand layout, descriptors and
+ * tensor-memory path of the split-precision transform passes.  n a multiple of
+ * 16 in [16, 128], k 64 or 128; all pointers device memory; *err (device int)
+ * is raised if the completion wait times out.  Asynchronous on `stream`. */
+PH_API int32_t ph_tc_selftest(float *d, const uint16_t *a, const uint16_t *b, int32_t n, int32_t k, int32_t fp16,
+                              int32_t *err, void *stream);
 
 /* ---- context -------------------------------------------------------------- */
 

@@ -23,6 +23,7 @@
 
 #include "ph_ctx.h"
 #include "ph_launch.cuh"
+#include "ph_pass_tc.cuh"
 
 // The serving runtime: lanes (stream + scratch), the transfer-function cache
 // and the tickets of requests in flight.
@@ -499,6 +500,36 @@ int get_twiddles(ph_ctx *ctx, int n, cudaStream_t s, const float2 **out) {
     return PH_OK;
 }
 
+// The tables of the tensor-core pass for (n, form), built on the host in FP64
+// once per context and kept on the device.
+int get_tc_table(ph_ctx *ctx, int n, int form, cudaStream_t s, const unsigned char **out) {
+    const int key = 8 * n + form;
+    auto it = ctx->tc_tables.find(key);
+    if (it != ctx->tc_tables.end()) {
+        *out = static_cast<const unsigned char *>(it->second);
+        return PH_OK;
+    }
+    if (capturing(s)) {
+        set_err(ctx, "tensor-core tables for length %d must be created outside a stream capture; call ph_reserve first",
+                n);
+        return PH_ERR_INVALID;
+    }
+    const size_t bytes = recon_b_tc_table_bytes(n, form);
+    std::vector<unsigned char> img(bytes);
+    recon_b_tc_build_table(n, form, img.data());
+    void *p = nullptr;
+    PH_CUDA(cudaMalloc(&p, bytes), "cudaMalloc(tensor-core tables)");
+    const cudaError_t e = cudaMemcpyAsync(p, img.data(), bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) cudaStreamSynchronize(s);   // the host image goes out of scope
+    if (e != cudaSuccess) {
+        cudaFree(p);
+        return cuda_status(ctx, e, "cudaMemcpyAsync(tensor-core tables)");
+    }
+    ctx->tc_tables[key] = p;
+    *out = static_cast<const unsigned char *>(p);
+    return PH_OK;
+}
+
 int check_len(ph_ctx *ctx, int nx, int ny) {
     if (nx <= 0 || ny <= 0) {
         set_err(ctx, "array sizes must be positive. Got (%d, %d).", nx, ny);
@@ -747,13 +778,17 @@ int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void 
     auto *p64 = packed != nullptr ? packed : at<unsigned long long>(ctx, L.p64);
     float2 *t = at<float2>(ctx, L.t);
     const bool want_proj = (kind == RK_PROJ) || proj != nullptr || argmin != nullptr;
+    if (kind == RK_PROJ && ctx->opt_form != PH_FORM_FP32 && recon_b_tc_supported(nx, (int)ctx->opt_form)) {
+        const unsigned char *tab = nullptr;
+        PH_TRY(get_tc_table(ctx, nx, (int)ctx->opt_form, s, &tab));
+    }
     char key[512];
     uint32_t thr_bits = 0;
     memcpy(&thr_bits, &threshold, sizeof thr_bits);
-    snprintf(key, sizeof key, "recon|%d|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%d|%p|%08x|%p|%d|%d", (int)kind, nin_x,
+    snprintf(key, sizeof key, "recon|%d|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%d|%p|%08x|%p|%d|%d|%d", (int)kind, nin_x,
              nin_y, slices, L.batch, vol_dtype, (void *)proj, (void *)argmin, vol, (const void *)wf, (const void *)hf,
              (const void *)hdz, ctx->scratch, (int)ctx->opt_loop_limit, (const void *)lpf, thr_bits, (void *)packed,
-             (int)accumulate, first);
+             (int)accumulate, first, (int)ctx->opt_form);
     return run_graph(ctx, s, key, [&](cudaStream_t s) -> int {
         PH_TRY(issue_spectrum(ctx, wf, hf, hdz, nx, ny, padded, nin_x, nin_y, at<float2>(ctx, L.a1), state, tw_x,
                               tw_y, at<double>(ctx, L.acc), at<float2>(ctx, L.mean), s, nullptr, lpf));
@@ -818,7 +853,13 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
         a.group = group;
         a.err = static_cast<int *>(ctx->small);
         PH_TRY(pass(ctx, s, "recon_a",[&] { return launch_recon_a(ny, a, nb, s); }));
-        if (kind == RK_PROJ) {
+        if (kind == RK_PROJ && ctx->opt_form != PH_FORM_FP32 && recon_b_tc_supported(nx, (int)ctx->opt_form)) {
+            ReconBTc b{};
+            PH_TRY(get_tc_table(ctx, nx, (int)ctx->opt_form, s, &b.table));
+            b.t = t; b.proj64 = p64; b.rows = ny_out; b.k0 = k0; b.nbatch = nb; b.group = group;
+            b.err = static_cast<int *>(ctx->small);
+            PH_TRY(pass(ctx, s, "recon_b_tc", [&] { return launch_recon_b_tc(nx, (int)ctx->opt_form, b, s); }));
+        } else if (kind == RK_PROJ) {
             ReconB<EPI_PROJ> b{};
             b.t = t; b.tw = tw_x; b.proj64 = p64; b.rows = ny_out; b.nx_out = nx_out; b.x0 = 0;
             b.k0 = k0; b.nbatch = nb; b.group = group; b.vol_slice_stride = (long long)nx_out * ny_out;
@@ -1046,6 +1087,7 @@ void ph_destroy(ph_ctx *ctx) {
         }
         for (auto e : ctx->prof_pool) cudaEventDestroy(e);
         for (auto &kv : ctx->tw) cudaFree(kv.second);
+        for (auto &kv : ctx->tc_tables) cudaFree(kv.second);
         if (ctx->scratch) cudaFree(ctx->scratch);
         if (ctx->small) cudaFree(ctx->small);
         if (ctx->phase_tab) cudaFree(ctx->phase_tab);
@@ -1069,6 +1111,10 @@ int32_t ph_set_option(ph_ctx *ctx, int32_t option, int64_t value) {
             ctx->opt_loop_limit = value;
             return PH_OK;
         case PH_OPT_PROFILE: ctx->opt_profile = value; return PH_OK;
+        case PH_OPT_FORM:
+            if (value < PH_FORM_FP32 || value > PH_FORM_FP16X2) break;
+            ctx->opt_form = value;
+            return PH_OK;
     }
     set_err(ctx, "unknown option %d", option);
     return PH_ERR_INVALID;

@@ -32,6 +32,10 @@ struct ph_ctx {
     // twiddle tables W_N^i, i in [0, N), one per transform length
     std::unordered_map<int, float2 *> tw;
 
+    // tables of the split-precision tensor-core pass (DFT matrices, twiddles),
+    // one per (length, form): key 8 n + form
+    std::unordered_map<int, void *> tc_tables;
+
     // scratch arena (grown on demand, never shrunk until destroy)
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
@@ -57,6 +61,7 @@ struct ph_ctx {
     int64_t opt_use_graphs = 1;
     int64_t opt_loop_limit = int64_t(1) << 20;
     int64_t opt_profile = 0;
+    int64_t opt_form = 0;           // PH_FORM_*: arithmetic of the projection's row pass
 
     // profiler: pending event pairs and a pool of spare events
     std::vector<ph_prof_record> prof;

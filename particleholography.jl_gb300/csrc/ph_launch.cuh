@@ -157,5 +157,12 @@ bool gs_row_staged(int n);
 bool gs_col_staged(int n);
 cudaError_t launch_gs_row_t(int n, const GsRowMidT &b, cudaStream_t s);
 cudaError_t launch_gs_col_t(int n, const GsColT &b, cudaStream_t s);
+// Split-precision tensor-core pass B (ph_pass_tc.cuh) for the projection.
+struct ReconBTc;
+bool recon_b_tc_supported(int n, int form);
+size_t recon_b_tc_table_bytes(int n, int form);
+int recon_b_tc_rows(int n, int form);
+void recon_b_tc_build_table(int n, int form, unsigned char *img);
+cudaError_t launch_recon_b_tc(int n, int form, const ReconBTc &p, cudaStream_t s);
 
 }  // namespace ph

@@ -1,0 +1,324 @@
+// ph_pass_tc.cuh -- the split-precision tensor-core form of reconstruction
+// pass B: rows y of the slice intermediate T, inverse DFT along kx as two
+// small complex DFT GEMMs on the 5th-generation tensor cores, |u|^2 and the
+// running min / argmin per pixel.
+//
+// Length N = N1 N2 (N1, N2 in {32, 64}).  With n = n1 + N1 n2 and
+// k = k2 + N2 k1 (W_m = exp(+2 pi i / m), the inverse transform):
+//   GEMM 1   Y[n1][k2]  = sum_n2 x[n1 + N1 n2] W_N2^(n2 k2)      (DFT-N2 per n1)
+//   twiddle  Y'[n1][k2] = Y[n1][k2] W_N^(n1 k2)                    (CUDA cores, FP32)
+//   GEMM 3   X[k2 + N2 k1] = sum_n1 Y'[n1][k2] W_N1^(n1 k1)        (DFT-N1 per k2)
+// Complex products are real GEMMs over interleaved (re, im): the data row
+// (re, im, re, im ...) is the A operand, K-major, and the DFT matrix F becomes
+// the real B operand [2k + c'][2n + c] = [[Fr, -Fi], [Fi, Fr]] so that
+// D[m][2k] = Re(x F), D[m][2k + 1] = Im(x F).
+//
+// Split precision: every operand v is held as v_hi + v_lo (16-bit each, v_hi =
+// round(v), v_lo = round(v - v_hi)) and a product is accumulated in FP32 from
+// A_hi B_hi + A_lo B_hi + A_hi B_lo (TERMS = 3; A_lo B_lo is below FP32
+// rounding) or from A_hi B_hi + A_lo B_hi (TERMS = 2: the matrix in one 16-bit
+// word).  BF16 keeps FP32's exponent range; FP16 has 3 more significant bits
+// per word and a tile is scaled by a power of two so that its largest value
+// is at most 2^9 (GEMM 1 grows it by at most N2 sqrt 2 < 2^15.5, inside FP16).
+//
+// A CTA (256 threads, one per SM: 224 KB of shared memory at N = 2048) owns
+// ROWS = 128 / N2 consecutive rows y and walks the slices of its group; one
+// tile is those rows of one slice.  GEMM 1 takes 128 / N1 rows per MMA chain
+// (HALVES chains per tile), GEMM 3 the whole tile.  The MMAs of one tile run
+// while the CUDA cores split the next tile's rows (GEMM 3) or reduce the
+// previous tile (GEMM 1):
+//   per slice b:  [twiddle + split D1(b) -> A3]  GEMM3(b)  [load + split x(b+1) -> A1]
+//                 GEMM1(b+1)  [|D3(b)|^2 -> min]
+//
+// Tables (built on the host in FP64, copied in one bulk copy per CTA): B1 and
+// B3 as swizzled K-major tiles (hi, then lo when TERMS = 3), then the twiddles
+// W_N^(n1 k2) as FP32 complex [k2][n1].
+#pragma once
+
+#include <cuda_fp16.h>
+#include "ph_common.cuh"
+#include "ph_tc.cuh"
+
+namespace ph {
+
+enum TcForm { TC_FP32 = 0, TC_BF16X3 = 1, TC_FP16X3 = 2, TC_FP16X2 = 3 };
+
+__host__ __device__ constexpr bool tc_form_fp16(int form) { return form == TC_FP16X3 || form == TC_FP16X2; }
+__host__ __device__ constexpr int tc_form_terms(int form) { return form == TC_FP16X2 ? 2 : 3; }
+
+template <int N1_, int N2_, int FORM_>
+struct TcPlan {
+    static constexpr int N1 = N1_, N2 = N2_, N = N1 * N2, FORM = FORM_;
+    static constexpr bool FP16 = tc_form_fp16(FORM);
+    static constexpr int TERMS = tc_form_terms(FORM);
+    static constexpr int BTERMS = TERMS == 3 ? 2 : 1;          // matrix words: hi (+ lo)
+    static constexpr int K1 = 2 * N2, NN1 = 2 * N2;            // GEMM 1: K, N (real)
+    static constexpr int K3 = 2 * N1, NN3 = 2 * N1;            // GEMM 3: K, N (real)
+    static constexpr int ROWS1 = 128 / N1;                     // rows per GEMM 1 chain
+    static constexpr int ROWS = 128 / N2;                      // rows per tile
+    static constexpr int HALVES = ROWS / ROWS1;                // GEMM 1 chains per tile
+    static constexpr int THREADS = 256;
+    // shared-memory layout (bytes; every tile on a 1024-byte boundary)
+    static constexpr uint32_t B1_BYTES = tc::sw128_bytes(NN1, K1);
+    static constexpr uint32_t B3_BYTES = tc::sw128_bytes(NN3, K3);
+    static constexpr uint32_t A1_BYTES = tc::sw128_bytes(128, K1);   // one chain, one word
+    static constexpr uint32_t A3_BYTES = tc::sw128_bytes(128, K3);
+    static constexpr uint32_t TW_BYTES = (uint32_t)N * 8;
+    static constexpr uint32_t OFF_B1 = 0;
+    static constexpr uint32_t OFF_B3 = OFF_B1 + BTERMS * B1_BYTES;
+    static constexpr uint32_t OFF_TW = OFF_B3 + BTERMS * B3_BYTES;
+    static constexpr uint32_t TABLE_BYTES = OFF_TW + TW_BYTES;        // the global image
+    static constexpr uint32_t OFF_A1 = (TABLE_BYTES + 1023) / 1024 * 1024;
+    static constexpr uint32_t OFF_A3 = OFF_A1 + 2 * HALVES * A1_BYTES;  // hi, lo per chain
+    static constexpr uint32_t OFF_BAR = OFF_A3 + 2 * A3_BYTES;
+    static constexpr uint32_t SMEM = OFF_BAR + 64 + 1024;              // + alignment slack
+    static constexpr uint32_t TMEM_COLS = 256;                          // D1 (HALVES x NN1) + D3 (NN3)
+    static_assert(HALVES * NN1 + NN3 <= (int)TMEM_COLS, "tensor memory");
+    static_assert(N1 % 32 == 0 && N2 % 32 == 0 && N1 <= 64 && N2 <= 64, "N1, N2 in {32, 64}");
+    static_assert(SMEM <= 227 * 1024, "shared memory");
+    // epilogue: each of the two warps on a lane quarter takes half of D3's columns
+    static constexpr int PIX = N1 / 2;                                  // pixels per thread
+};
+
+struct ReconBTc {
+    const float2 *t;                 // [batch][rows][n]
+    const unsigned char *table;      // TcPlan::TABLE_BYTES, 16-byte aligned
+    unsigned long long *proj64;      // [rows][n]
+    int *err;
+    int rows, k0, nbatch, group;
+};
+
+// 16-bit words of (x0, x1) in the form's type: hi and lo.
+template <bool FP16>
+__device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_t &lo) {
+    if constexpr (FP16) {
+        tc::split_f16x2(x0, x1, hi, lo);
+    } else {
+        tc::split_bf16x2(x0, x1, hi, lo);
+    }
+}
+
+template <class PL>
+__global__ void __launch_bounds__(256, 1) k_recon_b_tc(const ReconBTc p) {
+    constexpr int N = PL::N, N1 = PL::N1, N2 = PL::N2;
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem =
+        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + PL::OFF_BAR);   // [0] table, [1] GEMM 1, [2] GEMM 3
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 4);
+    float *smax = reinterpret_cast<float *>(bars + 5);                    // [8] per-warp maxima (FP16 forms)
+    const float2 *tw = reinterpret_cast<const float2 *>(smem + PL::OFF_TW);
+
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int quarter = warp & 3;                 // tensor-memory lane quarter of this warp
+    const int yb = blockIdx.x * PL::ROWS;
+    const int b0 = blockIdx.y * p.group;
+    const int b1 = min(b0 + p.group, p.nbatch);
+    if (b0 >= b1) return;
+
+    if (warp == 0) tc::tmem_alloc(tslot, PL::TMEM_COLS);
+    if (t == 0) {
+        mbar_init(bars + 0, 1);
+        mbar_init(bars + 1, 1);
+        mbar_init(bars + 2, 1);
+        mbar_fence_init();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t d1 = tmem;                              // HALVES x NN1 columns
+    const uint32_t d3 = tmem + PL::HALVES * PL::NN1;       // NN3 columns
+    if (t == 0) {
+        mbar_arrive_expect_tx(bars + 0, PL::TABLE_BYTES);
+        // (the image is a multiple of 16 bytes; one bulk copy per 64 KB piece)
+        for (uint32_t o = 0; o < PL::TABLE_BYTES; o += 65536u) {
+            const uint32_t sz = PL::TABLE_BYTES - o < 65536u ? PL::TABLE_BYTES - o : 65536u;
+            bulk_g2s(smem + o, p.table + o, sz, bars + 0);
+        }
+    }
+
+    // ---- GEMM 1 operands: thread -> (chain h, A1 row m = N1 r + n1, n2 range)
+    constexpr int WPQ1 = 2 / PL::HALVES;           // warps per (chain, lane quarter)
+    const int h1 = PL::HALVES == 2 ? (warp >> 2) : 0;
+    const int m1 = quarter * 32 + lane;            // A1 / D1 row
+    const int r1 = m1 / N1, n1 = m1 % N1;
+    const int row1 = h1 * PL::ROWS1 + r1;          // row of the tile
+    constexpr int N2W = N2 / WPQ1;                 // n2 values this thread splits
+    const int n2a = PL::HALVES == 2 ? 0 : (warp >> 2) * N2W;
+    const bool valid1 = yb + row1 < p.rows;
+
+    float scale = 1.0f;                            // FP16: power-of-two tile scale
+
+    auto load_split = [&](int b) {                 // rows of slice b -> A1 (hi, lo)
+        const float2 *src = p.t + ((size_t)b * p.rows + (valid1 ? yb + row1 : 0)) * N;
+        float2 v[N2W];
+#pragma unroll
+        for (int i = 0; i < N2W; ++i) v[i] = valid1 ? __ldcs(src + n1 + N1 * (n2a + i)) : make_float2(0.f, 0.f);
+        if constexpr (PL::FP16) {
+            float mx = 0.0f;
+#pragma unroll
+            for (int i = 0; i < N2W; ++i) mx = fmaxf(mx, fmaxf(fabsf(v[i].x), fabsf(v[i].y)));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            if (lane == 0) smax[warp] = mx;
+            __syncthreads();
+            mx = smax[0];
+#pragma unroll
+            for (int w = 1; w < 8; ++w) mx = fmaxf(mx, smax[w]);
+            int e = 0;
+            frexpf(mx, &e);                         // mx < 2^e
+            scale = mx > 0.0f ? ldexpf(1.0f, 9 - e) : 1.0f;
+#pragma unroll
+            for (int i = 0; i < N2W; ++i) v[i] = make_float2(v[i].x * scale, v[i].y * scale);
+        }
+        unsigned char *ahi = smem + PL::OFF_A1 + (2 * h1) * PL::A1_BYTES;
+        unsigned char *alo = ahi + PL::A1_BYTES;
+        // K index 2 n2 + c; 4 n2 (8 words of 16 bits) per 16-byte chunk
+#pragma unroll
+        for (int i = 0; i < N2W; i += 4) {
+            uint4 hv, lv;
+            split2<PL::FP16>(v[i].x, v[i].y, hv.x, lv.x);
+            split2<PL::FP16>(v[i + 1].x, v[i + 1].y, hv.y, lv.y);
+            split2<PL::FP16>(v[i + 2].x, v[i + 2].y, hv.z, lv.z);
+            split2<PL::FP16>(v[i + 3].x, v[i + 3].y, hv.w, lv.w);
+            const uint32_t off = tc::sw128_offset(128, m1, 2 * (n2a + i));
+            *reinterpret_cast<uint4 *>(ahi + off) = hv;
+            *reinterpret_cast<uint4 *>(alo + off) = lv;
+        }
+    };
+
+    auto issue_gemm1 = [&]() {                     // one thread
+        constexpr uint32_t idesc = tc::idesc_f16(128, PL::NN1, !PL::FP16);
+#pragma unroll
+        for (int h = 0; h < PL::HALVES; ++h) {
+            const uint32_t ahi = smem_addr(smem + PL::OFF_A1 + (2 * h) * PL::A1_BYTES);
+            const uint32_t alo = ahi + PL::A1_BYTES;
+            const uint32_t bhi = smem_addr(smem + PL::OFF_B1);
+            const uint32_t blo = bhi + PL::B1_BYTES;
+            int i = 0;
+#pragma unroll
+            for (int s = 0; s < PL::K1 / 16; ++s) {
+                const uint32_t oa = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
+                const uint32_t ob = (uint32_t)((s >> 2) * PL::NN1 * 128 + (s & 3) * 32);
+                const uint32_t d = d1 + (uint32_t)(h * PL::NN1);
+                tc::mma_f16(d, tc::desc_sw128(ahi + oa), tc::desc_sw128(bhi + ob), idesc, i++ > 0);
+                tc::mma_f16(d, tc::desc_sw128(alo + oa), tc::desc_sw128(bhi + ob), idesc, true);
+                if constexpr (PL::TERMS == 3) tc::mma_f16(d, tc::desc_sw128(ahi + oa), tc::desc_sw128(blo + ob), idesc, true);
+            }
+        }
+        tc::mma_commit(bars + 1);
+    };
+
+    auto issue_gemm3 = [&]() {
+        constexpr uint32_t idesc = tc::idesc_f16(128, PL::NN3, !PL::FP16);
+        const uint32_t ahi = smem_addr(smem + PL::OFF_A3);
+        const uint32_t alo = ahi + PL::A3_BYTES;
+        const uint32_t bhi = smem_addr(smem + PL::OFF_B3);
+        const uint32_t blo = bhi + PL::B3_BYTES;
+#pragma unroll
+        for (int s = 0; s < PL::K3 / 16; ++s) {
+            const uint32_t oa = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
+            const uint32_t ob = (uint32_t)((s >> 2) * PL::NN3 * 128 + (s & 3) * 32);
+            tc::mma_f16(d3, tc::desc_sw128(ahi + oa), tc::desc_sw128(bhi + ob), idesc, s > 0);
+            tc::mma_f16(d3, tc::desc_sw128(alo + oa), tc::desc_sw128(bhi + ob), idesc, true);
+            if constexpr (PL::TERMS == 3) tc::mma_f16(d3, tc::desc_sw128(ahi + oa), tc::desc_sw128(blo + ob), idesc, true);
+        }
+        tc::mma_commit(bars + 2);
+    };
+
+    // operand writes by every thread -> visible to the tensor core, then one thread issues
+    auto publish = [&]() {
+        fence_proxy_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+    };
+
+    // ---- twiddle + split: D1 -> A3.  Thread -> (chain h1, D1 lane m1, k2 range)
+    constexpr int K2W = N2 / WPQ1;
+    const int k2a = PL::HALVES == 2 ? 0 : (warp >> 2) * K2W;
+    auto twiddle_split = [&]() {
+        unsigned char *ahi = smem + PL::OFF_A3;
+        unsigned char *alo = ahi + PL::A3_BYTES;
+        const uint32_t taddr = d1 + (uint32_t)(h1 * PL::NN1) + ((uint32_t)(quarter * 32) << 16);
+#pragma unroll
+        for (int c = 0; c < K2W; c += 8) {          // 8 k2 = 16 columns per load
+            float v[16];
+            tc::tmem_ld16(taddr + (uint32_t)(2 * (k2a + c)), v);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int k2 = k2a + c + i;
+                const float2 w = tw[k2 * N1 + n1];
+                const float2 y = cmul(make_float2(v[2 * i], v[2 * i + 1]), w);
+                uint32_t hw, lw;
+                split2<PL::FP16>(y.x, y.y, hw, lw);
+                const uint32_t off = tc::sw128_offset(128, N2 * row1 + k2, 2 * n1);
+                *reinterpret_cast<uint32_t *>(ahi + off) = hw;
+                *reinterpret_cast<uint32_t *>(alo + off) = lw;
+            }
+        }
+    };
+
+    // ---- epilogue: D3 lane m3 = N2 R + k2; this warp's half of the columns
+    const int m3 = quarter * 32 + lane;
+    const int row3 = m3 / N2, k2e = m3 % N2;
+    const int k1a = (warp >> 2) * PL::PIX;
+    const bool valid3 = yb + row3 < p.rows;
+    float minv[PL::PIX];
+    int mink[PL::PIX];
+#pragma unroll
+    for (int i = 0; i < PL::PIX; ++i) { minv[i] = __int_as_float(0x7f800000); mink[i] = 0; }
+    auto reduce = [&](int k, float inv_s2) {
+        const uint32_t taddr = d3 + (uint32_t)(2 * k1a) + ((uint32_t)(quarter * 32) << 16);
+#pragma unroll
+        for (int c = 0; c < PL::PIX; c += 8) {
+            float v[16];
+            tc::tmem_ld16(taddr + (uint32_t)(2 * c), v);
+            tc::tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                float i2 = fmaf(v[2 * i], v[2 * i], v[2 * i + 1] * v[2 * i + 1]);
+                if constexpr (PL::FP16) i2 *= inv_s2;
+                if (i2 < minv[c + i]) { minv[c + i] = i2; mink[c + i] = k; }
+            }
+        }
+    };
+
+    uint32_t ph1 = 0, ph3 = 0;
+    mbar_wait(bars + 0, 0, p.err);                // tables in shared memory
+    load_split(b0);
+    float scale_cur = scale;
+    publish();
+    if (t == 0) issue_gemm1();
+    for (int b = b0; b < b1; ++b) {
+        mbar_wait(bars + 1, ph1, p.err);           // GEMM 1 of slice b done: D1 ready, A1 free
+        ph1 ^= 1u;
+        tc::fence_after_sync();
+        twiddle_split();
+        publish();
+        if (t == 0) issue_gemm3();
+        const float s_b = scale_cur;
+        if (b + 1 < b1) {
+            load_split(b + 1);
+            scale_cur = scale;
+            publish();
+            if (t == 0) issue_gemm1();
+        }
+        mbar_wait(bars + 2, ph3, p.err);           // GEMM 3 of slice b done: D3 ready, A3 free
+        ph3 ^= 1u;
+        tc::fence_after_sync();
+        reduce(p.k0 + b, 1.0f / (s_b * s_b));
+        tc::fence_before_sync();
+    }
+    if (valid3) {
+        unsigned long long *out = p.proj64 + (size_t)(yb + row3) * N;
+#pragma unroll
+        for (int i = 0; i < PL::PIX; ++i) atomicMin(out + k2e + N2 * (k1a + i), pack_min(minv[i], mink[i]));
+    }
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, PL::TMEM_COLS);
+}
+
+}  // namespace ph
