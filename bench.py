@@ -262,10 +262,12 @@ def cufft_standin(cfg: dict, h1, h2, hf, hdz, hp, hpi, frames: int) -> dict:
                     "per-slice host loop; GS + projection, labeling excluded), same GPU and inputs"}
 
 
-def sample_accuracy(ctx, cfg, h1, h2, hp, hpi, hf, hdz, outs, gs_iters, slices, s) -> dict:
+def sample_accuracy(ctx, cfg, h1, h2, hp, hpi, hf, hdz, outs, gs_iters, slices, s, form: int = 0) -> dict:
     """Our device path on the CPU baseline's sample (same holograms, GS
-    iterations and slices), compared with the oracle outputs of that sample."""
+    iterations and slices), compared with the oracle outputs of that sample;
+    `form` selects the arithmetic of the projection's row pass (PH_FORM_*)."""
     import torch
+    from ph_gb300 import _lib
     n = cfg["n"]
     dev = h1.device
     wf = torch.empty((n, n), dtype=torch.complex64, device=dev)
@@ -277,9 +279,13 @@ def sample_accuracy(ctx, cfg, h1, h2, hp, hpi, hf, hdz, outs, gs_iters, slices, 
         ctx.call("ph_gabor_wavefront", wf.data_ptr(), h1.data_ptr(), n, n, s)
     proj = torch.empty((n, n), dtype=torch.float32, device=dev)
     arg = torch.empty((n, n), dtype=torch.int32, device=dev)
-    ctx.call("ph_reconst_xyproj", proj.data_ptr(), arg.data_ptr(), wf.data_ptr(), hf.data.data_ptr(),
-             hdz.data.data_ptr(), n, n, slices, s)
-    torch.cuda.synchronize()
+    ctx.set_option(_lib.PH_OPT_FORM, form)
+    try:
+        ctx.call("ph_reconst_xyproj", proj.data_ptr(), arg.data_ptr(), wf.data_ptr(), hf.data.data_ptr(),
+                 hdz.data.data_ptr(), n, n, slices, s)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_option(_lib.PH_OPT_FORM, 0)
 
     w, p, a = wf.cpu().numpy(), proj.cpu().numpy(), arg.cpu().numpy()
     acc = {"against": "oracle FP32 (reference semantics) on the same sample",
@@ -338,6 +344,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--no-standin", action="store_true", help="skip the cuFFT stand-in of the reference sequence")
+    ap.add_argument("--no-forms", action="store_true", help="skip the tensor-core forms of the row pass")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
 
@@ -540,6 +547,53 @@ def main():
                "accuracy": sample_accuracy(ctx, cfg, h1, h2, hp, hpi, hf, hdz, outs, 2 if cfg["gs_iters"] else 0,
                                            16, s)}
 
+    # ---- the split-precision tensor-core forms of the projection's row pass, same frame
+    forms = None
+    if not args.no_forms and world == 1:
+        forms = {"fp32": {"ms_per_frame": round(total_ms / args.steps, 3), "mvoxel_s": round(value, 2),
+                          "p99_frame_ms": round(float(np.percentile(step_ms, 99)), 3),
+                          "recon_b_ms": kernels.get("recon_b", {}).get("ms_per_launch") if kernels else None}}
+        if cpu is not None:
+            forms["fp32"]["accuracy"] = _form_accuracy(cpu["accuracy"])
+        for name, code in (("bf16x3", _lib.PH_FORM_BF16X3), ("fp16x3", _lib.PH_FORM_FP16X3),
+                           ("fp16x2", _lib.PH_FORM_FP16X2)):
+            ctx.set_option(_lib.PH_OPT_FORM, code)
+            try:
+                for _ in range(2):
+                    frame(h1, h2)
+                torch.cuda.synchronize()
+                nf = min(args.steps, 20)
+                fev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nf)]
+                for i in range(nf):
+                    flush.zero_()
+                    fev[i][0].record(stream)
+                    frame(h1, h2)
+                    fev[i][1].record(stream)
+                torch.cuda.synchronize()
+                fms = [a.elapsed_time(b) for a, b in fev]
+                ctx.set_option(_lib.PH_OPT_PROFILE, 1)
+                ctx.profile_report()
+                for _ in range(3):
+                    flush.zero_()
+                    frame(h1, h2)
+                torch.cuda.synchronize()
+                fprof = ctx.profile_report()
+                ctx.set_option(_lib.PH_OPT_PROFILE, 0)
+            finally:
+                ctx.set_option(_lib.PH_OPT_FORM, 0)
+            tcb = fprof.get("recon_b_tc")
+            forms[name] = {"ms_per_frame": round(statistics.mean(fms), 3),
+                           "mvoxel_s": round(voxels / (statistics.mean(fms) / 1e3) / 1e6, 2),
+                           "p99_frame_ms": round(float(np.percentile(fms, 99)), 3), "frames": nf,
+                           "recon_b_ms": round(tcb[1] / tcb[0], 4) if tcb else None}
+            if cpu is not None:
+                acc = sample_accuracy(ctx, cfg, h1, h2, hp, hpi, hf, hdz, outs, 2 if cfg["gs_iters"] else 0, 16, s,
+                                      form=code)
+                forms[name]["accuracy"] = _form_accuracy(acc)
+        forms["note"] = ("tensor-core forms replace the projection's row pass (pass B) by two complex DFT GEMMs "
+                         "on tcgen05 (FP32 accumulation, hi + lo operands); pass A, GS and labeling stay FP32. "
+                         "accuracy: the CPU sample (2 GS iterations, 16 slices) against the FP32 and FP64 oracles")
+
     line = {
         "metric": "reconstructed Mvoxel/s + p99 frame latency, chosen vs plain FP32 form, 1 GB300",
         "value": round(value, 2), "unit": "Mvoxel/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -559,12 +613,22 @@ def main():
         "cpu_baseline": cpu,
         "e2e": e2e,
         "cufft_standin": standin,
+        "forms": forms,
         "clocks": clk,
     }
     print(json.dumps(line))
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def _form_accuracy(acc: dict) -> dict:
+    """The figures of one form's sample accuracy that the forms table reports."""
+    f64 = acc.get("vs_fp64", {})
+    return {"projection_rel_l2_vs_fp32_oracle": acc["projection_rel_l2"],
+            "argmin_agreement_vs_fp32_oracle": acc["argmin_agreement"],
+            "projection_rel_l2_vs_fp64": f64.get("projection_rel_l2"),
+            "argmin_agreement_vs_fp64": f64.get("argmin_agreement")}
 
 
 def _traffic_from_profiles(kernel: str, config: str):

@@ -286,18 +286,23 @@ __global__ void __launch_bounds__(256, 1) k_recon_b_tc(const ReconBTc p) {
         }
     };
 
+    // A wait that gives up raises p.err; the CTA then stops after its next
+    // barrier (every thread reads the flag there), so a copy or an MMA that
+    // never completes costs one bounded wait per CTA, not one per slice.
+    const volatile int *errv = p.err;
     uint32_t ph1 = 0, ph3 = 0;
     mbar_wait(bars + 0, 0, p.err);                // tables in shared memory
     load_split(b0);
     float scale_cur = scale;
     publish();
-    if (t == 0) issue_gemm1();
+    if (t == 0 && *errv == 0) issue_gemm1();
     for (int b = b0; b < b1; ++b) {
         mbar_wait(bars + 1, ph1, p.err);           // GEMM 1 of slice b done: D1 ready, A1 free
         ph1 ^= 1u;
         tc::fence_after_sync();
         twiddle_split();
         publish();
+        if (*errv != 0) break;                     // uniform: read by every thread after the barrier
         if (t == 0) issue_gemm3();
         const float s_b = scale_cur;
         if (b + 1 < b1) {
