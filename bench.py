@@ -109,6 +109,7 @@ def algorithmic_bytes(name: str, cfg: dict, launches: int, slices_per_frame: int
     per_frame = {
         "recon_a": 8.0 * n2 * slices_per_frame,
         "recon_b": 8.0 * n2 * slices_per_frame,
+        "recon_b_tc": 8.0 * n2 * slices_per_frame,
     }
     if name in per_frame:
         return per_frame[name] / max(1, launches)
@@ -345,6 +346,8 @@ def main():
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--no-standin", action="store_true", help="skip the cuFFT stand-in of the reference sequence")
     ap.add_argument("--no-forms", action="store_true", help="skip the tensor-core forms of the row pass")
+    ap.add_argument("--form", default="fp32", choices=["fp32", "bf16x3", "fp16x3", "fp16x2"],
+                    help="arithmetic of the projection's row pass in the timed frames")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
 
@@ -410,6 +413,9 @@ def main():
                  hdz.data.data_ptr(), n, n, S, s)
         ctx.call("ph_binarize_le", binary.data_ptr(), proj.data_ptr(), n * n, float(cfg["threshold"]), s)
         ctx.call("ph_ccl", labels.data_ptr(), binary.data_ptr(), _lib.PH_BOOL, n, n, s)
+
+    form_code = {"fp32": 0, "bf16x3": 1, "fp16x3": 2, "fp16x2": 3}[args.form]
+    ctx.set_option(_lib.PH_OPT_FORM, form_code)
 
     # ---- device-resident timing
     for _ in range(args.warmup):
@@ -513,7 +519,7 @@ def main():
     hbm, peak_kind = _peaks()
     kernels = {}
     for name, (cnt, ms) in prof.items():
-        b = algorithmic_bytes(name, cfg, cnt, S * prof_steps) if name in ("recon_a", "recon_b") else \
+        b = algorithmic_bytes(name, cfg, cnt, S * prof_steps) if name in ("recon_a", "recon_b", "recon_b_tc") else \
             algorithmic_bytes(name, cfg, cnt, S)
         per_launch_ms = ms / cnt
         gbs = (b / (per_launch_ms / 1e3) / 1e9) if b else None
@@ -549,7 +555,7 @@ def main():
 
     # ---- the split-precision tensor-core forms of the projection's row pass, same frame
     forms = None
-    if not args.no_forms and world == 1:
+    if not args.no_forms and world == 1 and form_code == 0:
         forms = {"fp32": {"ms_per_frame": round(total_ms / args.steps, 3), "mvoxel_s": round(value, 2),
                           "p99_frame_ms": round(float(np.percentile(step_ms, 99)), 3),
                           "recon_b_ms": kernels.get("recon_b", {}).get("ms_per_launch") if kernels else None}}
@@ -600,7 +606,8 @@ def main():
         "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded disc holograms generated on the device)",
         "config": {"workload": cfg["workload"], "n": n, "slices": S, "dz_um": cfg["dz"], "z0_um": cfg["z0"],
-                   "gs_iterations": cfg["gs_iters"], "discs": cfg["discs"], "form": "fp32-stockham",
+                   "gs_iterations": cfg["gs_iters"], "discs": cfg["discs"],
+                   "form": "fp32-stockham" if form_code == 0 else f"{args.form}-tcgen05 row pass",
                    "l2": "flushed (512 MiB write) before every timed step",
                    "kernel_timing": f"{prof_steps} further steps with per-pass CUDA events on the launching stream "
                                     "(graph replay off); the frame time is taken without them",

@@ -11,14 +11,19 @@ that the CUDA implementation can be checked against it:
   seeded synthetic-hologram generator used for small parity cases.
 * ``ccl``           -- the Playne-Hawick label-equivalence CCL of ``ccl.jl``
   restated in plain C (``ccl_ref.c``), compiled with gcc and loaded by ctypes.
+* ``detect_ref``    -- the reference's 3-D detection bookkeeping (per-slice
+  rectangles, particle neighbourhoods, Tamura depth and centre of mass), the
+  checker of the end-to-end detection case below.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
 ``--impl reference`` legs of ``bench.py`` may import this package, and only as
 the checker or the timed CPU baseline.  The product path never calls it.
 
-Parity status: the FFT / transfer / Gerchberg-Saxton / reconstruction rows are
-pinned only by golden vectors this oracle generates (the reference's tests hold
-no numeric values for them and its FFT is the closed cuFFT library); the CCL row
-is pinned by the reference's own known answer (84 components on
-``test/data/binaryparticles.png``).
+Parity status: pinned to the reference's own output.  The reference's
+end-to-end detection test (``test/runtests.jl:153-193``) wrote
+``test/data/particles.json`` (22 particles) from its cuFFT path; this oracle
+run on the same inputs reproduces all 22 (same slice, x and y to one Float32
+ulp), which pins its transfer functions, Gerchberg-Saxton, reconstruction and
+N0f8 rounding.  The CCL row is also pinned by the reference's known answer (84
+components on ``test/data/binaryparticles.png``).
 """
