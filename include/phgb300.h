@@ -306,13 +306,17 @@ PH_API void ph_batch_destroy(ph_batch *batch);
 /* ---- serving --------------------------------------------------------------------- */
 
 /* A request queue in front of cu_get_reconst_xyprojection (holofunc.jl:248-266)
- * for a stream of holograms.  The server owns `lanes` CUDA streams, each with
- * scratch for the largest request it accepts; a request goes to the lane with
- * the fewest requests in flight and runs there asynchronously.  The transfer
- * functions are built as the reference builds them (cu_transfer_sqrt_arr +
- * cu_transfer, holofunc.jl:30-67) for Hf = H(-z0) and Hdz = H(-dz) and kept in
- * an LRU cache keyed by (size, distance, wavelength, pitch), so recurring
- * optics reuse them.  One request: */
+ * for a stream of holograms, with continuous admission under an HBM budget.
+ * The server owns one scratch pool (its budget) and `lanes` work slots, each a
+ * CUDA stream.  A request needs one block of the pool (its reconstruction
+ * scratch, sized for its own shape and slice count) and a free slot; requests
+ * are admitted in arrival order as slots and memory free up, and queue until
+ * then.  Admitted requests run concurrently on their slots' streams.  A block
+ * and its slot return to the server when the request's completion callback has
+ * run.  The transfer functions are built as the reference builds them
+ * (cu_transfer_sqrt_arr + cu_transfer, holofunc.jl:30-67) for Hf = H(-z0) and
+ * Hdz = H(-dz) and kept in an LRU cache keyed by (size, distance, wavelength,
+ * pitch), so recurring optics reuse them.  One request: */
 typedef struct ph_serve_request {
     const float *hologram;   /* Float32 [n_slow][n_fast]; wavefront = sqrt(hologram) + 0i */
     float *proj;             /* out: minimum over slices of |u|^2 */
@@ -320,6 +324,19 @@ typedef struct ph_serve_request {
     int32_t n_fast, n_slow, slices;
     double z0, dz;           /* micrometres: first slice at z0, then steps of dz */
     double wavlen, dx;       /* micrometres */
+    /* Device ingest (nullable frame; hologram is then ignored): the hologram is
+     * made on the device from an 8-bit camera frame, as load_gray2float
+     * (utils.jl:23-25), the background removal of the reference's
+     * preprocessing docs (img .- bkg .+ offset) and pad_with_mean
+     * (utils.jl:319-325) make it on the host.  The frame is row-major
+     * [frame_n_fast rows][frame_pitch bytes] (a camera or BMP image: the
+     * image's row is the Julia array's first index), frame_channels 1 or 3
+     * equal channels (the first is read), rows bottom-up when frame_flip.
+     * A frame smaller than n_fast x n_slow is centred and padded with its mean. */
+    const uint8_t *frame;
+    int32_t frame_n_fast, frame_n_slow, frame_pitch, frame_channels, frame_flip;
+    const double *background;   /* nullable: Float64 [frame_n_slow][frame_n_fast] (make_background) */
+    double background_offset;   /* added after the subtraction (the docs use 64/255) */
 } ph_serve_request;
 
 typedef struct ph_server ph_server;
@@ -327,20 +344,30 @@ typedef struct ph_server ph_server;
 enum { PH_PENDING = 9 };   /* ph_serve_poll: the request has not finished */
 
 /* Creates a server for requests up to max_n_fast x max_n_slow x max_slices
- * (reconstruction of holofunc.jl:248-266; allocates the lanes' scratch). */
+ * (reconstruction of holofunc.jl:248-266).  scratch_budget_bytes is the pool
+ * requests are admitted against (0 = lanes x the largest request's block); it
+ * must hold at least one largest request. */
 PH_API int32_t ph_serve_create(ph_ctx *ctx, int32_t lanes, int32_t max_n_fast, int32_t max_n_slow,
-                               int32_t max_slices, int32_t tf_cache_entries, ph_server **out);
+                               int32_t max_slices, int32_t tf_cache_entries, size_t scratch_budget_bytes,
+                               ph_server **out);
 /* Queues one cu_get_reconst_xyprojection (holofunc.jl:248-266) request and
- * returns at once with its ticket.  The request runs after the work already
- * queued on `stream` (the one that wrote the hologram).  The hologram and
- * outputs must stay valid until the request has finished.  Thread-safe; one
- * poller per ticket. */
+ * returns at once with its ticket; it is admitted at once when a slot and its
+ * block are free, else when earlier requests finish.  The request runs after
+ * the work queued on `stream` before this call (the work that wrote its
+ * inputs).  Inputs and outputs must stay valid until it has finished.
+ * Thread-safe; one poller per ticket. */
 PH_API int32_t ph_serve_submit(ph_server *srv, const ph_serve_request *req, int64_t *ticket, void *stream);
 /* PH_OK when the request has finished (the ticket is then released and
- * *latency_ms, if non-NULL, is submission to completion), PH_PENDING if not yet
- * (wait = 0), or waits for it (wait = 1).  No reference counterpart. */
+ * *latency_ms, if non-NULL, is submission to completion, queueing included),
+ * PH_PENDING if not yet (wait = 0), or waits for it (wait = 1), admitting
+ * queued requests as earlier ones finish.  No reference counterpart. */
 PH_API int32_t ph_serve_poll(ph_server *srv, int64_t ticket, int32_t wait, double *latency_ms);
-/* Waits for every request, frees the server (no reference counterpart). */
+/* Requests queued and running, pool bytes in use and at peak, and the number of
+ * requests that had to queue at submission (each pointer nullable).
+ * (no reference counterpart) */
+PH_API int32_t ph_serve_stats(ph_server *srv, int64_t *queued, int64_t *running, size_t *bytes_in_use,
+                              size_t *bytes_peak, int64_t *waited);
+/* Runs every queued request to completion, frees the server (no reference counterpart). */
 PH_API void ph_serve_destroy(ph_server *srv);
 
 /* ---- preprocessing ------------------------------------------------------------- */

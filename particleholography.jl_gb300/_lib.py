@@ -88,7 +88,8 @@ SIGNATURES = {
     "ph_batch_run": (_i32, [_vp, _vp]),
     "ph_batch_scratch_bytes": (_sz, [_vp]),
     "ph_batch_destroy": (None, [_vp]),
-    "ph_serve_create": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, ctypes.POINTER(_vp)]),
+    "ph_serve_create": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _sz, ctypes.POINTER(_vp)]),
+    "ph_serve_stats": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_sz), ctypes.POINTER(_sz), ctypes.POINTER(_i64)]),
     "ph_serve_submit": (_i32, [_vp, _vp, ctypes.POINTER(_i64), _vp]),
     "ph_serve_poll": (_i32, [_vp, _i64, _i32, ctypes.POINTER(_f64)]),
     "ph_serve_destroy": (None, [_vp]),
@@ -103,7 +104,9 @@ PH_PENDING = 9
 class ServeRequest(ctypes.Structure):
     """ph_serve_request (phgb300.h)."""
     _fields_ = [("hologram", _vp), ("proj", _vp), ("argmin", _vp), ("n_fast", _i32), ("n_slow", _i32),
-                ("slices", _i32), ("z0", _f64), ("dz", _f64), ("wavlen", _f64), ("dx", _f64)]
+                ("slices", _i32), ("z0", _f64), ("dz", _f64), ("wavlen", _f64), ("dx", _f64),
+                ("frame", _vp), ("frame_n_fast", _i32), ("frame_n_slow", _i32), ("frame_pitch", _i32),
+                ("frame_channels", _i32), ("frame_flip", _i32), ("background", _vp), ("background_offset", _f64)]
 
 
 class ReconItem(ctypes.Structure):

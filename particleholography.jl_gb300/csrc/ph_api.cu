@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <deque>
 #include <cmath>
 #include <map>
 #include <thread>
@@ -25,14 +26,21 @@
 #include "ph_launch.cuh"
 #include "ph_pass_tc.cuh"
 
-// The serving runtime: lanes (stream + scratch), the transfer-function cache
-// and the tickets of requests in flight.
+// The serving runtime: work slots (one CUDA stream each), a scratch pool
+// sub-allocated per request under the server's HBM budget, the queue of
+// requests waiting for a slot and memory, and the transfer-function cache.
+struct ph_server;
 struct ph_serve_ticket {
+    int64_t id = 0;
+    ph_serve_request req{};
+    ph_server *srv = nullptr;
     std::atomic<int> done{0};
-    double t_submit = 0.0, t_done = 0.0;   // seconds, steady clock
-    cudaEvent_t ev = nullptr;              // completes after the host callback ran
-    int lane = 0;
-    std::atomic<int> *lane_inflight = nullptr;
+    double t_submit = 0.0, t_admit = 0.0, t_done = 0.0;   // seconds, steady clock
+    cudaEvent_t submitted = nullptr;   // on the caller's stream at submission: the inputs are written
+    cudaEvent_t ev = nullptr;          // on the slot's stream after the completion callback
+    int slot = -1;                     // -1 while queued
+    size_t off = 0, bytes = 0;         // the request's block of the pool
+    bool harvested = false;            // its slot and block have been given back
 };
 
 struct ph_serve_tf {
@@ -44,21 +52,24 @@ struct ph_serve_tf {
 
 struct ph_server {
     ph_ctx *ctx = nullptr;
-    std::mutex mu;
+    std::mutex mu;                         // queue, pool, slots, tickets, cache
     int lanes = 1;
     int max_nx = 0, max_ny = 0, max_slices = 0;
-    size_t lane_bytes = 0;
-    void *scratch = nullptr;               // lanes x lane_bytes (+ d_sqr buffers)
+    size_t pool_bytes = 0, used = 0, peak = 0;
+    void *pool = nullptr;
+    std::map<size_t, size_t> free_blocks;  // offset -> bytes, coalesced
     std::vector<cudaStream_t> streams;
-    std::vector<std::atomic<int>> inflight;
+    std::vector<ph_serve_ticket *> slot_job;   // nullptr = free
+    std::deque<ph_serve_ticket *> pending;     // FIFO, admitted from the front
+    std::mutex cmu;                            // completions, written by host callbacks
+    std::vector<ph_serve_ticket *> completed;
     std::map<std::tuple<int, int, double, double, double>, ph_serve_tf> tfs;
     int tf_cap = 16;
     uint64_t clock = 0;
     int64_t next_ticket = 1;
     std::unordered_map<int64_t, ph_serve_ticket *> tickets;
     std::vector<cudaEvent_t> event_pool;
-    cudaEvent_t order = nullptr;           // orders a lane after the submitting stream
-    explicit ph_server(int n) : inflight(n) {}
+    int64_t admitted_total = 0, waited_total = 0;   // requests admitted; of them, ones that had to queue
 };
 
 // A planned batch of reconstructions: its items, lanes, own scratch and the
@@ -278,6 +289,47 @@ __global__ void k_pad_mean_fill(float *out, const float *in, const double *acc, 
     float v = (float)(acc[0] / n);
     if (xi >= 0 && xi < nin_f && yi >= 0 && yi < nin_s) v = in[(size_t)yi * nin_f + xi];
     out[(size_t)y * pad + x] = v;
+}
+
+// Device ingest of an 8-bit camera frame: load_gray2float (utils.jl:23-25,
+// level / 255 as Float32) of the frame stored row-major [row][col] (pitch
+// bytes, `channels` interleaved equal channels, the first read; rows bottom-up
+// when flip), written in the library's layout out[col][row] (the Julia buffer
+// of the image: its first index, the row, is contiguous), then the background
+// removal of the preprocessing docs, img .- bkg .+ offset in FP64 stored as
+// Float32.  With acc, the FP64 sum of the result is accumulated (for
+// pad_with_mean).  32 x 32 tiles transposed through shared memory.
+__global__ void k_ingest_u8(float *out, const uint8_t *frame, int rows, int cols, int pitch, int channels, int flip,
+                            const double *bkg, double offset, double *acc) {
+    __shared__ float tile[32][33];
+    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;   // image row / column of the tile
+    const int tx = threadIdx.x, ty = threadIdx.y;           // block (32, 8)
+    for (int r = ty; r < 32; r += 8) {                      // read along columns of image row i0 + r
+        const int i = i0 + r, j = j0 + tx;
+        float v = 0.0f;
+        if (i < rows && j < cols) {
+            const int src_row = flip ? rows - 1 - i : i;
+            v = (float)frame[(size_t)src_row * pitch + (size_t)j * channels] / 255.0f;
+        }
+        tile[tx][r] = v;                                    // [column][row]
+    }
+    __syncthreads();
+    double sx = 0.0;
+    for (int c = ty; c < 32; c += 8) {                      // write along rows of column j0 + c
+        const int j = j0 + c, i = i0 + tx;
+        if (i < rows && j < cols) {
+            float v = tile[c][tx];
+            const size_t o = (size_t)j * rows + i;
+            if (bkg != nullptr) v = (float)((double)v - bkg[o] + offset);
+            out[o] = v;
+            sx += v;
+        }
+    }
+    if (acc != nullptr) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sx += __shfl_xor_sync(0xffffffffu, sx, o);
+        if (tx == 0) atomicAdd(acc, sx);
+    }
 }
 
 __global__ void k_proj_finish(const unsigned long long *p64, float *proj, int32_t *argmin, size_t n) {
@@ -936,8 +988,9 @@ double now_s() {
 void CUDART_CB serve_done(void *p) {   // host callback: no CUDA calls here
     auto *t = static_cast<ph_serve_ticket *>(p);
     t->t_done = now_s();
-    t->lane_inflight->fetch_sub(1);
     t->done.store(1, std::memory_order_release);
+    std::lock_guard<std::mutex> lk(t->srv->cmu);   // held briefly, never around a CUDA call
+    t->srv->completed.push_back(t);
 }
 
 cudaEvent_t serve_event(ph_server *srv) {
@@ -1659,8 +1712,164 @@ void ph_batch_destroy(ph_batch *batch) {
     delete batch;
 }
 
+// ---- serving: a block of the pool per request, admitted in arrival order
+namespace {
+
+// Bytes of one request's block: the reconstruction scratch (slice batches of
+// at most kLaneBatchBytes), the hologram made by the device ingest, the
+// transfer builder's square-root plane and the ingest's sum.
+size_t serve_request_bytes(ph_ctx *ctx, int nx, int ny, int slices, ReconLayout *out = nullptr) {
+    const ReconLayout L = recon_layout(ctx, nx, ny, ny, nx, slices, kLaneBatchBytes);
+    if (out) *out = L;
+    const size_t plane = ((size_t)nx * ny * sizeof(float) + kAlign - 1) / kAlign * kAlign;
+    return (L.total + kAlign - 1) / kAlign * kAlign + 2 * plane + kAlign;
+}
+
+bool pool_alloc(ph_server *srv, size_t bytes, size_t *off) {
+    for (auto it = srv->free_blocks.begin(); it != srv->free_blocks.end(); ++it) {
+        if (it->second >= bytes) {
+            *off = it->first;
+            const size_t rest = it->second - bytes;
+            const size_t next = it->first + bytes;
+            srv->free_blocks.erase(it);
+            if (rest) srv->free_blocks[next] = rest;
+            srv->used += bytes;
+            srv->peak = std::max(srv->peak, srv->used);
+            return true;
+        }
+    }
+    return false;
+}
+
+void pool_free(ph_server *srv, size_t off, size_t bytes) {
+    srv->used -= bytes;
+    auto it = srv->free_blocks.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != srv->free_blocks.end() && it->first + it->second == nx->first) {
+        it->second += nx->second;
+        srv->free_blocks.erase(nx);
+    }
+    if (it != srv->free_blocks.begin()) {
+        auto pv = std::prev(it);
+        if (pv->first + pv->second == it->first) {
+            pv->second += it->second;
+            srv->free_blocks.erase(it);
+        }
+    }
+}
+
+// Gives back the slot and block of every request whose completion callback has run.
+void serve_harvest(ph_server *srv) {
+    std::vector<ph_serve_ticket *> done;
+    {
+        std::lock_guard<std::mutex> lk(srv->cmu);
+        done.swap(srv->completed);
+    }
+    for (auto *t : done) {
+        if (t->harvested) continue;
+        pool_free(srv, t->off, t->bytes);
+        srv->slot_job[t->slot] = nullptr;
+        t->harvested = true;
+    }
+}
+
+// Issues one admitted request on its slot's stream.
+int serve_issue(ph_server *srv, ph_serve_ticket *t) {
+    ph_ctx *ctx = srv->ctx;
+    const ph_serve_request *req = &t->req;
+    const int nx = req->n_fast, ny = req->n_slow;
+    cudaStream_t ls = srv->streams[t->slot];
+    PH_CUDA(cudaStreamWaitEvent(ls, t->submitted, 0), "cudaStreamWaitEvent");
+    ReconLayout L{};
+    serve_request_bytes(ctx, nx, ny, req->slices, &L);
+    char *base = static_cast<char *>(srv->pool) + t->off;
+    const size_t plane = ((size_t)nx * ny * sizeof(float) + kAlign - 1) / kAlign * kAlign;
+    const size_t recon_end = (L.total + kAlign - 1) / kAlign * kAlign;
+    float *holo_buf = reinterpret_cast<float *>(base + recon_end);
+    float *dsqr = reinterpret_cast<float *>(base + recon_end + plane);
+    double *acc = reinterpret_cast<double *>(base + recon_end + 2 * plane);
+    for (int n : {nx, ny}) {   // a new twiddle table is complete before any slot reads it
+        if (ctx->tw.find(n) == ctx->tw.end()) {
+            const float2 *tw = nullptr;
+            PH_TRY(get_twiddles(ctx, n, ls, &tw));
+            PH_CUDA(cudaStreamSynchronize(ls), "cudaStreamSynchronize");
+        }
+    }
+    const float2 *tw_x = ctx->tw[nx], *tw_y = ctx->tw[ny];
+    const float2 *hf = nullptr, *hdz = nullptr;
+    ph_serve_tf *ef = nullptr, *ed = nullptr;
+    PH_TRY(serve_transfer(srv, ls, dsqr, nx, ny, req->z0, req->wavlen, req->dx, &hf, &ef));
+    PH_TRY(serve_transfer(srv, ls, dsqr, nx, ny, req->dz, req->wavlen, req->dx, &hdz, &ed));
+    const float *holo = req->hologram;
+    if (req->frame != nullptr) {   // device ingest: decode, background, mean padding
+        const int fr = req->frame_n_fast, fc = req->frame_n_slow;
+        const bool pad = fr != nx || fc != ny;
+        float *img = pad ? reinterpret_cast<float *>(base + L.t) : holo_buf;   // T is free until the passes
+        PH_CUDA(cudaMemsetAsync(acc, 0, sizeof(double), ls), "cudaMemsetAsync");
+        dim3 b(32, 8), g((fr + 31) / 32, (fc + 31) / 32);
+        k_ingest_u8<<<g, b, 0, ls>>>(img, req->frame, fr, fc, req->frame_pitch, req->frame_channels, req->frame_flip,
+                                     req->background, req->background_offset, pad ? acc : nullptr);
+        PH_TRY(launched(ctx, cudaGetLastError(), "ingest"));
+        if (pad) {
+            dim3 bp(32, 8);
+            k_pad_mean_fill<<<grid2d(nx, ny, bp), bp, 0, ls>>>(holo_buf, img, acc, (double)fr * fc, fr, fc, nx,
+                                                               nx / 2 - fr / 2, ny / 2 - fc / 2);
+            PH_TRY(launched(ctx, cudaGetLastError(), "ingest padding"));
+        }
+        holo = holo_buf;
+    }
+    auto *state = reinterpret_cast<float4 *>(base + L.state);
+    auto *p64 = reinterpret_cast<unsigned long long *>(base + L.p64);
+    PH_TRY(issue_spectrum(ctx, nullptr, hf, hdz, nx, ny, false, nx, ny, reinterpret_cast<float2 *>(base + L.a1), state,
+                          tw_x, tw_y, reinterpret_cast<double *>(base + L.acc), reinterpret_cast<float2 *>(base + L.mean),
+                          ls, holo));
+    PH_CUDA(cudaMemsetAsync(p64, 0xff, sizeof(unsigned long long) * nx * ny, ls), "cudaMemsetAsync");
+    PH_TRY(issue_recon_slices(ctx, RK_PROJ, req->proj, req->argmin, nullptr, PH_F32, nx, ny, nx, ny, 0, 0,
+                              req->slices, L.batch, state, reinterpret_cast<float2 *>(base + L.t), p64, tw_x, tw_y,
+                              true, ls));
+    cudaEventRecord(ef->last_use, ls);
+    cudaEventRecord(ed->last_use, ls);
+    PH_CUDA(cudaLaunchHostFunc(ls, serve_done, t), "cudaLaunchHostFunc");
+    PH_CUDA(cudaEventRecord(t->ev, ls), "cudaEventRecord");
+    return PH_OK;
+}
+
+// Harvests completions, then admits queued requests in arrival order while a
+// slot is free and the pool holds the next request's block.  The caller holds
+// srv->mu and ctx->mu.
+int serve_dispatch(ph_server *srv) {
+    serve_harvest(srv);
+    while (!srv->pending.empty()) {
+        ph_serve_ticket *t = srv->pending.front();
+        int slot = -1;
+        for (int l = 0; l < srv->lanes; ++l)
+            if (srv->slot_job[l] == nullptr) { slot = l; break; }
+        if (slot < 0) return PH_OK;
+        size_t off = 0;
+        if (!pool_alloc(srv, t->bytes, &off)) return PH_OK;   // waits for memory to free up
+        srv->pending.pop_front();
+        t->slot = slot;
+        t->off = off;
+        t->t_admit = now_s();
+        srv->slot_job[slot] = t;
+        ++srv->admitted_total;
+        const int st = serve_issue(srv, t);
+        if (st != PH_OK) {
+            // the request failed to issue: give its block and slot back and report it
+            pool_free(srv, t->off, t->bytes);
+            srv->slot_job[slot] = nullptr;
+            t->harvested = true;
+            t->done.store(-1, std::memory_order_release);
+            return st;
+        }
+    }
+    return PH_OK;
+}
+
+}  // namespace
+
 int32_t ph_serve_create(ph_ctx *ctx, int32_t lanes, int32_t max_n_fast, int32_t max_n_slow, int32_t max_slices,
-                        int32_t tf_cache_entries, ph_server **out) {
+                        int32_t tf_cache_entries, size_t scratch_budget_bytes, ph_server **out) {
     PH_ENTER(ctx, nullptr);
     PH_NONNULL(out, "out");
     *out = nullptr;
@@ -1668,39 +1877,41 @@ int32_t ph_serve_create(ph_ctx *ctx, int32_t lanes, int32_t max_n_fast, int32_t 
     if (max_slices < 1) { set_err(ctx, "max_slices must be >= 1. Got %d.", max_slices); return PH_ERR_SIZE; }
     if (tf_cache_entries < 2) { set_err(ctx, "the transfer cache needs at least 2 entries"); return PH_ERR_INVALID; }
     PH_TRY(check_len(ctx, max_n_fast, max_n_slow));
-    auto *srv = new ph_server(lanes);
+    const size_t largest = serve_request_bytes(ctx, max_n_fast, max_n_slow, max_slices);
+    const size_t total = scratch_budget_bytes ? scratch_budget_bytes : largest * lanes;
+    if (total < largest) {
+        set_err(ctx, "a scratch budget of %zu bytes holds no request of the largest size (%zu bytes)", total, largest);
+        return PH_ERR_OOM;
+    }
+    if (ctx->budget && total + ctx->scratch_bytes > ctx->budget) {
+        set_err(ctx, "server scratch of %zu bytes exceeds the context's HBM budget of %zu bytes", total, ctx->budget);
+        return PH_ERR_OOM;
+    }
+    auto *srv = new ph_server();
     srv->ctx = ctx;
     srv->lanes = lanes;
     srv->max_nx = max_n_fast;
     srv->max_ny = max_n_slow;
     srv->max_slices = max_slices;
     srv->tf_cap = tf_cache_entries;
-    const ReconLayout L = recon_layout(ctx, max_n_fast, max_n_slow, max_n_slow, max_n_fast, max_slices,
-                                       kLaneBatchBytes);
-    srv->lane_bytes = (L.total + kAlign - 1) / kAlign * kAlign +
-                      ((size_t)max_n_fast * max_n_slow * sizeof(float) + kAlign - 1) / kAlign * kAlign;
-    const size_t total = srv->lane_bytes * lanes;
+    srv->pool_bytes = total;
     auto fail = [&](int code) {
         for (auto x : srv->streams) if (x) cudaStreamDestroy(x);
-        if (srv->order) cudaEventDestroy(srv->order);
-        if (srv->scratch) cudaFree(srv->scratch);
+        if (srv->pool) cudaFree(srv->pool);
         delete srv;
         cudaGetLastError();
         return code;
     };
-    if (ctx->budget && total + ctx->scratch_bytes > ctx->budget) {
-        set_err(ctx, "server scratch of %zu bytes exceeds the context's HBM budget of %zu bytes", total, ctx->budget);
-        return fail(PH_ERR_OOM);
-    }
-    if (cudaMalloc(&srv->scratch, total) != cudaSuccess) {
+    if (cudaMalloc(&srv->pool, total) != cudaSuccess) {
         set_err(ctx, "cudaMalloc of %zu bytes of server scratch failed", total);
         return fail(PH_ERR_OOM);
     }
+    srv->free_blocks[0] = total;
     srv->streams.assign(lanes, nullptr);
-    if (cudaEventCreateWithFlags(&srv->order, cudaEventDisableTiming) != cudaSuccess) return fail(PH_ERR_CUDA);
+    srv->slot_job.assign(lanes, nullptr);
     for (int l = 0; l < lanes; ++l) {
         if (cudaStreamCreateWithFlags(&srv->streams[l], cudaStreamNonBlocking) != cudaSuccess) {
-            set_err(ctx, "could not create the server lanes");
+            set_err(ctx, "could not create the server's streams");
             return fail(PH_ERR_CUDA);
         }
     }
@@ -1715,100 +1926,129 @@ int32_t ph_serve_submit(ph_server *srv, const ph_serve_request *req, int64_t *ti
     std::lock_guard<std::mutex> clk(ctx->mu);
     DeviceGuard dg(ctx->device);
     const int nx = req->n_fast, ny = req->n_slow;
-    PH_NONNULL(req->hologram, "hologram");
+    if (req->frame == nullptr) PH_NONNULL(req->hologram, "hologram");
     if (req->proj == nullptr && req->argmin == nullptr) { set_err(ctx, "proj and argmin are both NULL"); return PH_ERR_INVALID; }
     if (req->slices < 1) { set_err(ctx, "slices must be >= 1. Got %d.", req->slices); return PH_ERR_SIZE; }
     PH_TRY(check_len(ctx, nx, ny));
-    const ReconLayout L = recon_layout(ctx, nx, ny, ny, nx, req->slices, kLaneBatchBytes);
-    const size_t dsqr_off = srv->lane_bytes - ((size_t)srv->max_nx * srv->max_ny * sizeof(float) + kAlign - 1) / kAlign * kAlign;
-    if (L.total > dsqr_off || (size_t)nx * ny > (size_t)srv->max_nx * srv->max_ny) {
+    if (req->frame != nullptr) {
+        const int fr = req->frame_n_fast, fc = req->frame_n_slow;
+        if (fr < 1 || fc < 1 || fr > nx || fc > ny || (req->frame_channels != 1 && req->frame_channels != 3) ||
+            req->frame_pitch < fc * req->frame_channels) {
+            set_err(ctx, "frame %d x %d (pitch %d, %d channels) does not fit the request %d x %d", fr, fc,
+                    req->frame_pitch, req->frame_channels, nx, ny);
+            return PH_ERR_SIZE;
+        }
+    }
+    if ((size_t)nx * ny > (size_t)srv->max_nx * srv->max_ny || req->slices > srv->max_slices) {
         set_err(ctx, "request %d x %d x %d exceeds the server's maximum %d x %d x %d", nx, ny, req->slices,
                 srv->max_nx, srv->max_ny, srv->max_slices);
         return PH_ERR_SIZE;
     }
-    // the lane with the fewest requests in flight
-    int lane = 0;
-    for (int l = 1; l < srv->lanes; ++l)
-        if (srv->inflight[l].load() < srv->inflight[lane].load()) lane = l;
-    cudaStream_t ls = srv->streams[lane];
-    // after the work already queued on the caller's stream (which wrote the hologram)
-    PH_CUDA(cudaEventRecord(srv->order, static_cast<cudaStream_t>(stream)), "cudaEventRecord");
-    PH_CUDA(cudaStreamWaitEvent(ls, srv->order, 0), "cudaStreamWaitEvent");
-    char *base = static_cast<char *>(srv->scratch) + (size_t)lane * srv->lane_bytes;
-    const float2 *tw_x = nullptr, *tw_y = nullptr;
-    for (int n : {nx, ny}) {   // a new twiddle table is complete before any lane reads it
-        if (ctx->tw.find(n) == ctx->tw.end()) {
-            const float2 *tw = nullptr;
-            PH_TRY(get_twiddles(ctx, n, ls, &tw));
-            PH_CUDA(cudaStreamSynchronize(ls), "cudaStreamSynchronize");
-        }
-    }
-    tw_x = ctx->tw[nx];
-    tw_y = ctx->tw[ny];
-    const float2 *hf = nullptr, *hdz = nullptr;
-    ph_serve_tf *ef = nullptr, *ed = nullptr;
-    float *dsqr = reinterpret_cast<float *>(base + dsqr_off);
-    PH_TRY(serve_transfer(srv, ls, dsqr, nx, ny, req->z0, req->wavlen, req->dx, &hf, &ef));
-    PH_TRY(serve_transfer(srv, ls, dsqr, nx, ny, req->dz, req->wavlen, req->dx, &hdz, &ed));
     auto *t = new ph_serve_ticket();
-    t->t_submit = now_s();
-    t->lane = lane;
-    t->lane_inflight = &srv->inflight[lane];
-    t->ev = serve_event(srv);
-    if (t->ev == nullptr) { delete t; set_err(ctx, "cudaEventCreate failed"); return PH_ERR_CUDA; }
-    auto *state = reinterpret_cast<float4 *>(base + L.state);
-    auto *p64 = reinterpret_cast<unsigned long long *>(base + L.p64);
-    int st = issue_spectrum(ctx, nullptr, hf, hdz, nx, ny, false, nx, ny, reinterpret_cast<float2 *>(base + L.a1),
-                            state, tw_x, tw_y, reinterpret_cast<double *>(base + L.acc),
-                            reinterpret_cast<float2 *>(base + L.mean), ls, req->hologram);
-    if (st == PH_OK && cudaMemsetAsync(p64, 0xff, sizeof(unsigned long long) * nx * ny, ls) != cudaSuccess)
-        st = cuda_status(ctx, cudaGetLastError(), "cudaMemsetAsync");
-    if (st == PH_OK)
-        st = issue_recon_slices(ctx, RK_PROJ, req->proj, req->argmin, nullptr, PH_F32, nx, ny, nx, ny, 0, 0,
-                                req->slices, L.batch, state, reinterpret_cast<float2 *>(base + L.t), p64, tw_x, tw_y,
-                                true, ls);
-    if (st != PH_OK) {
-        srv->event_pool.push_back(t->ev);
+    t->req = *req;
+    t->srv = srv;
+    t->bytes = serve_request_bytes(ctx, nx, ny, req->slices);
+    if (t->bytes > srv->pool_bytes) {
         delete t;
-        return st;
+        set_err(ctx, "request needs %zu bytes of scratch; the server holds %zu", t->bytes, srv->pool_bytes);
+        return PH_ERR_SIZE;
     }
-    cudaEventRecord(ef->last_use, ls);
-    cudaEventRecord(ed->last_use, ls);
-    srv->inflight[lane].fetch_add(1);
-    PH_CUDA(cudaLaunchHostFunc(ls, serve_done, t), "cudaLaunchHostFunc");
-    PH_CUDA(cudaEventRecord(t->ev, ls), "cudaEventRecord");
-    *ticket = srv->next_ticket++;
-    srv->tickets[*ticket] = t;
-    return PH_OK;
+    t->submitted = serve_event(srv);
+    t->ev = serve_event(srv);
+    if (t->submitted == nullptr || t->ev == nullptr) {
+        if (t->submitted) srv->event_pool.push_back(t->submitted);
+        if (t->ev) srv->event_pool.push_back(t->ev);
+        delete t;
+        set_err(ctx, "cudaEventCreate failed");
+        return PH_ERR_CUDA;
+    }
+    t->t_submit = now_s();
+    // the request runs after the work already queued on the caller's stream (which wrote its inputs)
+    PH_CUDA(cudaEventRecord(t->submitted, static_cast<cudaStream_t>(stream)), "cudaEventRecord");
+    t->id = srv->next_ticket++;
+    srv->tickets[t->id] = t;
+    srv->pending.push_back(t);
+    *ticket = t->id;
+    const int st = serve_dispatch(srv);
+    if (t->slot < 0 && t->done.load() == 0) ++srv->waited_total;   // queued for a slot or for memory
+    return st;
 }
 
 int32_t ph_serve_poll(ph_server *srv, int64_t ticket, int32_t wait, double *latency_ms) {
     if (srv == nullptr) return PH_ERR_INVALID;
-    ph_serve_ticket *t = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(srv->mu);
-        auto it = srv->tickets.find(ticket);
-        if (it == srv->tickets.end()) {
-            std::lock_guard<std::mutex> clk(srv->ctx->mu);
-            set_err(srv->ctx, "unknown ticket %lld", (long long)ticket);
+    ph_ctx *ctx = srv->ctx;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    auto it = srv->tickets.find(ticket);
+    if (it == srv->tickets.end()) {
+        std::lock_guard<std::mutex> clk(ctx->mu);
+        set_err(ctx, "unknown ticket %lld", (long long)ticket);
+        return PH_ERR_INVALID;
+    }
+    ph_serve_ticket *t = it->second;
+    for (;;) {
+        {
+            std::lock_guard<std::mutex> clk(ctx->mu);
+            DeviceGuard dg(ctx->device);
+            PH_TRY(serve_dispatch(srv));
+        }
+        if (t->done.load(std::memory_order_acquire) != 0) break;
+        if (!wait) return PH_PENDING;
+        // wait for this request if it runs, else for the oldest running one (which frees a slot and memory)
+        cudaEvent_t ev = nullptr;
+        if (t->slot >= 0) {
+            ev = t->ev;
+        } else {
+            double oldest = 1e300;
+            for (auto *j : srv->slot_job)
+                if (j != nullptr && j->t_admit < oldest) { oldest = j->t_admit; ev = j->ev; }
+        }
+        if (ev == nullptr) {
+            std::lock_guard<std::mutex> clk(ctx->mu);
+            set_err(ctx, "ticket %lld is queued but no request runs", (long long)ticket);
             return PH_ERR_INVALID;
         }
-        t = it->second;
-        if (!t->done.load(std::memory_order_acquire) && !wait) return PH_PENDING;
-    }
-    if (!t->done.load(std::memory_order_acquire)) {
-        DeviceGuard dg(srv->ctx->device);
-        const cudaError_t e = cudaEventSynchronize(t->ev);   // recorded after the callback
+        lk.unlock();
+        cudaError_t e;
+        {
+            DeviceGuard dg(ctx->device);
+            e = cudaEventSynchronize(ev);   // recorded after the completion callback
+        }
+        lk.lock();
         if (e != cudaSuccess) {
-            std::lock_guard<std::mutex> clk(srv->ctx->mu);
-            return cuda_status(srv->ctx, e, "cudaEventSynchronize");
+            std::lock_guard<std::mutex> clk(ctx->mu);
+            return cuda_status(ctx, e, "cudaEventSynchronize");
         }
     }
-    std::lock_guard<std::mutex> lk(srv->mu);
+    const int outcome = t->done.load(std::memory_order_acquire);
     if (latency_ms) *latency_ms = (t->t_done - t->t_submit) * 1e3;
     srv->event_pool.push_back(t->ev);
+    srv->event_pool.push_back(t->submitted);
     srv->tickets.erase(ticket);
     delete t;
+    if (outcome < 0) {
+        std::lock_guard<std::mutex> clk(ctx->mu);
+        set_err(ctx, "request %lld could not be issued", (long long)ticket);
+        return PH_ERR_CUDA;
+    }
+    return PH_OK;
+}
+
+int32_t ph_serve_stats(ph_server *srv, int64_t *queued, int64_t *running, size_t *bytes_in_use, size_t *bytes_peak,
+                       int64_t *waited) {
+    if (srv == nullptr) return PH_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    {
+        std::lock_guard<std::mutex> clk(srv->ctx->mu);
+        DeviceGuard dg(srv->ctx->device);
+        PH_TRY(serve_dispatch(srv));
+    }
+    int64_t run = 0;
+    for (auto *j : srv->slot_job) run += j != nullptr;
+    if (queued) *queued = (int64_t)srv->pending.size();
+    if (running) *running = run;
+    if (bytes_in_use) *bytes_in_use = srv->used;
+    if (bytes_peak) *bytes_peak = srv->peak;
+    if (waited) *waited = srv->waited_total;
     return PH_OK;
 }
 
@@ -1817,9 +2057,19 @@ void ph_serve_destroy(ph_server *srv) {
     {
         std::lock_guard<std::mutex> lk(srv->mu);
         DeviceGuard dg(srv->ctx->device);
-        for (auto x : srv->streams) cudaStreamSynchronize(x);
+        // every queued request is admitted and finished before the memory goes
+        for (;;) {
+            int st;
+            {
+                std::lock_guard<std::mutex> clk(srv->ctx->mu);
+                st = serve_dispatch(srv);
+            }
+            for (auto x : srv->streams) cudaStreamSynchronize(x);   // (the completion callbacks have run)
+            if (st != PH_OK || srv->pending.empty()) break;
+        }
         for (auto &kv : srv->tickets) {
             srv->event_pool.push_back(kv.second->ev);
+            srv->event_pool.push_back(kv.second->submitted);
             delete kv.second;
         }
         for (auto e : srv->event_pool) cudaEventDestroy(e);
@@ -1829,8 +2079,7 @@ void ph_serve_destroy(ph_server *srv) {
             cudaEventDestroy(kv.second.last_use);
         }
         for (auto x : srv->streams) cudaStreamDestroy(x);
-        if (srv->order) cudaEventDestroy(srv->order);
-        if (srv->scratch) cudaFree(srv->scratch);
+        if (srv->pool) cudaFree(srv->pool);
         cudaGetLastError();
     }
     delete srv;

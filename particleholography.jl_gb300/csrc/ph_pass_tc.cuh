@@ -243,12 +243,12 @@ __global__ void __launch_bounds__(256, 1) k_recon_b_tc(const ReconBTc p) {
         unsigned char *alo = ahi + PL::A3_BYTES;
         const uint32_t taddr = d1 + (uint32_t)(h1 * PL::NN1) + ((uint32_t)(quarter * 32) << 16);
 #pragma unroll
-        for (int c = 0; c < K2W; c += 8) {          // 8 k2 = 16 columns per load
-            float v[16];
-            tc::tmem_ld16(taddr + (uint32_t)(2 * (k2a + c)), v);
+        for (int c = 0; c < K2W; c += 16) {         // 16 k2 = 32 columns per load
+            float v[32];
+            tc::tmem_ld32(taddr + (uint32_t)(2 * (k2a + c)), v);
             tc::tmem_wait_ld();
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
+            for (int i = 0; i < 16; ++i) {
                 const int k2 = k2a + c + i;
                 const float2 w = tw[k2 * N1 + n1];
                 const float2 y = cmul(make_float2(v[2 * i], v[2 * i + 1]), w);
@@ -273,12 +273,12 @@ __global__ void __launch_bounds__(256, 1) k_recon_b_tc(const ReconBTc p) {
     auto reduce = [&](int k, float inv_s2) {
         const uint32_t taddr = d3 + (uint32_t)(2 * k1a) + ((uint32_t)(quarter * 32) << 16);
 #pragma unroll
-        for (int c = 0; c < PL::PIX; c += 8) {
-            float v[16];
-            tc::tmem_ld16(taddr + (uint32_t)(2 * c), v);
+        for (int c = 0; c < PL::PIX; c += 16) {
+            float v[32];
+            tc::tmem_ld32(taddr + (uint32_t)(2 * c), v);
             tc::tmem_wait_ld();
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
+            for (int i = 0; i < 16; ++i) {
                 float i2 = fmaf(v[2 * i], v[2 * i], v[2 * i + 1] * v[2 * i + 1]);
                 if constexpr (PL::FP16) i2 *= inv_s2;
                 if (i2 < minv[c + i]) { minv[c + i] = i2; mink[c + i] = k; }
@@ -290,6 +290,13 @@ __global__ void __launch_bounds__(256, 1) k_recon_b_tc(const ReconBTc p) {
     // barrier (every thread reads the flag there), so a copy or an MMA that
     // never completes costs one bounded wait per CTA, not one per slice.
     const volatile int *errv = p.err;
+    // The rows of a later slice are prefetched into L2 by the copy engine, so
+    // that the loads of load_split meet L2 rather than DRAM latency.
+    const uint32_t tile_bytes = (uint32_t)(min(PL::ROWS, p.rows - yb) * N * 8);
+    auto prefetch = [&](int b) {
+        if (t == 0 && b < b1) tc::prefetch_l2(p.t + ((size_t)b * p.rows + yb) * N, tile_bytes);
+    };
+    prefetch(b0 + 1);
     uint32_t ph1 = 0, ph3 = 0;
     mbar_wait(bars + 0, 0, p.err);                // tables in shared memory
     load_split(b0);
@@ -304,6 +311,7 @@ __global__ void __launch_bounds__(256, 1) k_recon_b_tc(const ReconBTc p) {
         publish();
         if (*errv != 0) break;                     // uniform: read by every thread after the barrier
         if (t == 0) issue_gemm3();
+        prefetch(b + 2);
         const float s_b = scale_cur;
         if (b + 1 < b1) {
             load_split(b + 1);

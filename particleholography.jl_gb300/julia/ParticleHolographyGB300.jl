@@ -442,6 +442,14 @@ struct _ServeRequest
     dz::Float64
     wavlen::Float64
     dx::Float64
+    frame::CuPtr{UInt8}          # device ingest of an 8-bit frame (CU_NULL: use hologram)
+    frame_n_fast::Int32
+    frame_n_slow::Int32
+    frame_pitch::Int32
+    frame_channels::Int32
+    frame_flip::Int32
+    background::CuPtr{Float64}
+    background_offset::Float64
 end
 
 mutable struct Server
@@ -449,11 +457,11 @@ mutable struct Server
     live::Dict{Int64,Any}
 end
 
-function Server(max_size::Tuple{Int,Int}, max_slices::Int; lanes::Int=3, tf_cache::Int=16)
+function Server(max_size::Tuple{Int,Int}, max_slices::Int; lanes::Int=3, tf_cache::Int=16, budget::Integer=0)
     h = Ref{Ptr{Cvoid}}(C_NULL)
     _check(ccall((:ph_serve_create, libphgb300), Int32,
-                 (Ptr{Cvoid}, Int32, Int32, Int32, Int32, Int32, Ref{Ptr{Cvoid}}),
-                 _ctx(), lanes, max_size[1], max_size[2], max_slices, tf_cache, h))
+                 (Ptr{Cvoid}, Int32, Int32, Int32, Int32, Int32, Csize_t, Ref{Ptr{Cvoid}}),
+                 _ctx(), lanes, max_size[1], max_size[2], max_slices, tf_cache, budget, h))
     s = Server(h[], Dict{Int64,Any}())
     finalizer(s) do x
         x.handle == C_NULL || ccall((:ph_serve_destroy, libphgb300), Cvoid, (Ptr{Cvoid},), x.handle)
@@ -465,7 +473,8 @@ end
 function submit!(s::Server, holo::CuArray{Float32,2}, proj::CuArray{Float32,2}, slices::Int, z0::Real, dz::Real;
                  wavlen::Real=0.6328, dx::Real=10.0, argmin::Union{Nothing,CuArray{Int32,2}}=nothing)
     req = Ref(_ServeRequest(pointer(holo), pointer(proj), argmin === nothing ? CU_NULL : pointer(argmin),
-                            size(holo, 1), size(holo, 2), slices, z0, dz, wavlen, dx))
+                            size(holo, 1), size(holo, 2), slices, z0, dz, wavlen, dx,
+                            CU_NULL, 0, 0, 0, 0, 0, CU_NULL, 0.0))
     t = Ref{Int64}(0)
     _check(ccall((:ph_serve_submit, libphgb300), Int32, (Ptr{Cvoid}, Ref{_ServeRequest}, Ref{Int64}, Ptr{Cvoid}),
                  s.handle, req, t, _stream()))

@@ -65,3 +65,72 @@ def test_rejects_oversize_and_bad_requests(ph, cuda):
     with pytest.raises(AssertionError):
         srv.submit(small, torch.empty((32, 64), dtype=torch.float32, device=cuda), 4, 1000.0, 100.0)
     srv.close()
+
+
+def _block_bytes(ph, cuda, n, slices):
+    """Pool bytes one n x n x slices request takes (the server's peak after it alone)."""
+    srv = ph.Server(max_shape=(n, n), max_slices=slices, lanes=1)
+    holo = torch.full((n, n), 0.5, dtype=torch.float32, device=cuda)
+    srv.poll(srv.submit(holo, torch.empty_like(holo), slices, 1000.0, 200.0), wait=True)
+    b = srv.stats()["bytes_peak"]
+    srv.close()
+    return b
+
+
+def test_requests_wait_for_budget_then_complete(ph, cuda):
+    """Admission against the HBM budget: with room for one request's scratch, the
+    later ones queue at submission and run as the earlier ones finish; every
+    result equals the single call."""
+    n, slices = 1024, 64
+    block = _block_bytes(ph, cuda, n, slices)
+    srv = ph.Server(max_shape=(n, n), max_slices=slices, lanes=4, budget_bytes=int(block * 1.5))
+    rng = np.random.default_rng(3)
+    reqs = []
+    for i in range(3):
+        holo = to_dev(rng.uniform(0.1, 1.0, (n, n)).astype(np.float32), cuda)
+        proj, arg = torch.empty_like(holo), torch.empty(holo.shape, dtype=torch.int32, device=cuda)
+        reqs.append((srv.submit(holo, proj, slices, 1000.0 + 100 * i, 200.0, argmin=arg), holo, proj, arg, i))
+    st = srv.stats()
+    assert st["waited"] == 2 and st["running"] + st["queued"] <= 3
+    for t, holo, proj, arg, i in reqs:
+        assert srv.poll(t, wait=True) > 0.0
+        p1, a1 = _single(ph, holo, slices, 1000.0 + 100 * i, 200.0)
+        assert torch.equal(proj, p1) and torch.equal(arg, a1)
+    st = srv.stats()
+    assert st["queued"] == 0 and st["running"] == 0 and st["bytes_in_use"] == 0
+    assert block <= st["bytes_peak"] <= block * 1.5
+    srv.close()
+
+
+def test_budget_below_one_request_is_rejected(ph, cuda):
+    with pytest.raises(MemoryError):
+        ph.Server(max_shape=(1024, 1024), max_slices=64, lanes=2, budget_bytes=1 << 20)
+
+
+@pytest.mark.parametrize("channels,flip", [(1, False), (3, True)])
+def test_frame_ingest_equals_host_preprocessing(ph, cuda, channels, flip):
+    """An 8-bit camera frame decoded, background-corrected and mean-padded on the
+    device in the serving loop gives the projection of the same steps done
+    beforehand (load_gray2float, img .- bkg .+ 64/255, pad_with_mean)."""
+    rows, cols, n, slices = 200, 180, 256, 12
+    rng = np.random.default_rng(11)
+    img = rng.integers(40, 220, (rows, cols), dtype=np.uint8)          # row-major camera frame
+    bkg = rng.uniform(0.3, 0.6, (cols, rows))                          # Float64, library layout
+    off = 64 / 255
+    # host-side steps, in the library layout (image row = fast index)
+    holo_small = ((img.T.astype(np.float32) / np.float32(255.0)).astype(np.float64) - bkg + off).astype(np.float32)
+    holo = ph.pad_with_mean(to_dev(holo_small, cuda), n)
+    p_ref, a_ref = _single(ph, holo, slices, 1000.0, 200.0)
+    frame = np.repeat(img[:, :, None], channels, axis=2) if channels == 3 else img
+    if flip:
+        frame = frame[::-1]
+    srv = ph.Server(max_shape=(n, n), max_slices=slices, lanes=2)
+    proj, arg = torch.empty((n, n), dtype=torch.float32, device=cuda), torch.empty((n, n), dtype=torch.int32,
+                                                                                   device=cuda)
+    t = srv.submit_frame(to_dev(np.ascontiguousarray(frame), cuda), proj, slices, 1000.0, 200.0, argmin=arg,
+                         background=to_dev(bkg, cuda), background_offset=off, flip=flip)
+    srv.poll(t, wait=True)
+    srv.close()
+    from phtest import rel_l2, to_np
+    assert rel_l2(to_np(proj), to_np(p_ref)) < 1e-6
+    assert np.mean(to_np(arg) == to_np(a_ref)) > 0.999
