@@ -57,7 +57,7 @@ struct TcPlan {
     static constexpr int ROWS1 = 128 / N1;                     // rows per GEMM 1 chain
     static constexpr int ROWS = 128 / N2;                      // rows per tile
     static constexpr int HALVES = ROWS / ROWS1;                // GEMM 1 chains per tile
-    static constexpr int THREADS = 256;
+    static constexpr int THREADS = 384;                      // 8 consumer + 4 producer warps
     // shared-memory layout (bytes; every tile on a 1024-byte boundary)
     static constexpr uint32_t B1_BYTES = tc::sw128_bytes(NN1, K1);
     static constexpr uint32_t B3_BYTES = tc::sw128_bytes(NN3, K3);
@@ -71,7 +71,7 @@ struct TcPlan {
     static constexpr uint32_t OFF_A1 = (TABLE_BYTES + 1023) / 1024 * 1024;
     static constexpr uint32_t OFF_A3 = OFF_A1 + 2 * HALVES * A1_BYTES;  // hi, lo per chain
     static constexpr uint32_t OFF_BAR = OFF_A3 + 2 * A3_BYTES;
-    static constexpr uint32_t SMEM = OFF_BAR + 64 + 1024;              // + alignment slack
+    static constexpr uint32_t SMEM = OFF_BAR + 128 + 1024;             // + alignment slack
     static constexpr uint32_t TMEM_COLS = 256;                          // D1 (HALVES x NN1) + D3 (NN3)
     static_assert(HALVES * NN1 + NN3 <= (int)TMEM_COLS, "tensor memory");
     static_assert(N1 % 32 == 0 && N2 % 32 == 0 && N1 <= 64 && N2 <= 64, "N1, N2 in {32, 64}");
@@ -98,19 +98,36 @@ __device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_
     }
 }
 
+// Warp roles (384 threads): warps 0-7 are the consumers (8 warps, two per
+// tensor-memory lane quarter), warps 8-11 the producers.
+//   producers, tile b:  wait GEMM 1 (b-1) done (A1 free) -> load + split the
+//                       rows of slice b into A1 -> barrier -> one thread waits
+//                       until the consumers have read D1 (b-1), issues GEMM 1 (b)
+//   consumers, tile b:  wait GEMM 1 (b) done -> twiddle + split D1 -> A3 ->
+//                       release D1 -> barrier -> one thread issues GEMM 3 (b) ->
+//                       wait GEMM 3 (b) done -> |D3|^2 -> running minimum
+// so the global loads of tile b + 1 run while the consumers work on tile b.
+// Hand-offs are mbarriers: GEMM 1 and GEMM 3 completion (tcgen05.commit), D1
+// released (256 consumer arrivals) and, for the FP16 forms, the row scales of
+// a tile (128 producer arrivals, two barriers alternating by tile parity so
+// that no waiter falls two phases behind).  Every wait is bounded.
+constexpr int kTcConsumers = 256, kTcProducers = 128;
+
 template <class PL>
-__global__ void __launch_bounds__(256, 1) k_recon_b_tc(const ReconBTc p) {
+__global__ void __launch_bounds__(384, 1) k_recon_b_tc(const ReconBTc p) {
     constexpr int N = PL::N, N1 = PL::N1, N2 = PL::N2;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem =
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + PL::OFF_BAR);   // [0] table, [1] GEMM 1, [2] GEMM 3
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 4);
-    float *smax = reinterpret_cast<float *>(bars + 5);                    // [8] per-warp maxima (FP16 forms)
+    // barriers: [0] tables, [1] GEMM 1 done, [2] GEMM 3 done, [3] D1 released, [4], [5] row scales
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + PL::OFF_BAR);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 6);
+    float *rmax = reinterpret_cast<float *>(bars + 7);          // [4 producer warps] per-warp row maxima
+    float *rscale = rmax + 4;                                    // [2][ROWS] per-row scales (FP16 forms)
     const float2 *tw = reinterpret_cast<const float2 *>(smem + PL::OFF_TW);
 
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int quarter = warp & 3;                 // tensor-memory lane quarter of this warp
+    const bool producer = warp >= 8;
     const int yb = blockIdx.x * PL::ROWS;
     const int b0 = blockIdx.y * p.group;
     const int b1 = min(b0 + p.group, p.nbatch);
@@ -121,6 +138,9 @@ __global__ void __launch_bounds__(256, 1) k_recon_b_tc(const ReconBTc p) {
         mbar_init(bars + 0, 1);
         mbar_init(bars + 1, 1);
         mbar_init(bars + 2, 1);
+        mbar_init(bars + 3, kTcConsumers);
+        mbar_init(bars + 4, kTcProducers);
+        mbar_init(bars + 5, kTcProducers);
         mbar_fence_init();
     }
     tc::fence_before_sync();
@@ -131,204 +151,204 @@ __global__ void __launch_bounds__(256, 1) k_recon_b_tc(const ReconBTc p) {
     const uint32_t d3 = tmem + PL::HALVES * PL::NN1;       // NN3 columns
     if (t == 0) {
         mbar_arrive_expect_tx(bars + 0, PL::TABLE_BYTES);
-        // (the image is a multiple of 16 bytes; one bulk copy per 64 KB piece)
         for (uint32_t o = 0; o < PL::TABLE_BYTES; o += 65536u) {
             const uint32_t sz = PL::TABLE_BYTES - o < 65536u ? PL::TABLE_BYTES - o : 65536u;
             bulk_g2s(smem + o, p.table + o, sz, bars + 0);
         }
     }
-
-    // ---- GEMM 1 operands: thread -> (chain h, A1 row m = N1 r + n1, n2 range)
-    constexpr int WPQ1 = 2 / PL::HALVES;           // warps per (chain, lane quarter)
-    const int h1 = PL::HALVES == 2 ? (warp >> 2) : 0;
-    const int m1 = quarter * 32 + lane;            // A1 / D1 row
-    const int r1 = m1 / N1, n1 = m1 % N1;
-    const int row1 = h1 * PL::ROWS1 + r1;          // row of the tile
-    constexpr int N2W = N2 / WPQ1;                 // n2 values this thread splits
-    const int n2a = PL::HALVES == 2 ? 0 : (warp >> 2) * N2W;
-    const bool valid1 = yb + row1 < p.rows;
-
-    float scale = 1.0f;                            // FP16: power-of-two tile scale
-
-    auto load_split = [&](int b) {                 // rows of slice b -> A1 (hi, lo)
-        const float2 *src = p.t + ((size_t)b * p.rows + (valid1 ? yb + row1 : 0)) * N;
-        float2 v[N2W];
-#pragma unroll
-        for (int i = 0; i < N2W; ++i) v[i] = valid1 ? __ldcs(src + n1 + N1 * (n2a + i)) : make_float2(0.f, 0.f);
-        if constexpr (PL::FP16) {
-            float mx = 0.0f;
-#pragma unroll
-            for (int i = 0; i < N2W; ++i) mx = fmaxf(mx, fmaxf(fabsf(v[i].x), fabsf(v[i].y)));
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            if (lane == 0) smax[warp] = mx;
-            __syncthreads();
-            mx = smax[0];
-#pragma unroll
-            for (int w = 1; w < 8; ++w) mx = fmaxf(mx, smax[w]);
-            int e = 0;
-            frexpf(mx, &e);                         // mx < 2^e
-            scale = mx > 0.0f ? ldexpf(1.0f, 9 - e) : 1.0f;
-#pragma unroll
-            for (int i = 0; i < N2W; ++i) v[i] = make_float2(v[i].x * scale, v[i].y * scale);
-        }
-        unsigned char *ahi = smem + PL::OFF_A1 + (2 * h1) * PL::A1_BYTES;
-        unsigned char *alo = ahi + PL::A1_BYTES;
-        // K index 2 n2 + c; 4 n2 (8 words of 16 bits) per 16-byte chunk
-#pragma unroll
-        for (int i = 0; i < N2W; i += 4) {
-            uint4 hv, lv;
-            split2<PL::FP16>(v[i].x, v[i].y, hv.x, lv.x);
-            split2<PL::FP16>(v[i + 1].x, v[i + 1].y, hv.y, lv.y);
-            split2<PL::FP16>(v[i + 2].x, v[i + 2].y, hv.z, lv.z);
-            split2<PL::FP16>(v[i + 3].x, v[i + 3].y, hv.w, lv.w);
-            const uint32_t off = tc::sw128_offset(128, m1, 2 * (n2a + i));
-            *reinterpret_cast<uint4 *>(ahi + off) = hv;
-            *reinterpret_cast<uint4 *>(alo + off) = lv;
-        }
-    };
-
-    auto issue_gemm1 = [&]() {                     // one thread
-        constexpr uint32_t idesc = tc::idesc_f16(128, PL::NN1, !PL::FP16);
-#pragma unroll
-        for (int h = 0; h < PL::HALVES; ++h) {
-            const uint32_t ahi = smem_addr(smem + PL::OFF_A1 + (2 * h) * PL::A1_BYTES);
-            const uint32_t alo = ahi + PL::A1_BYTES;
-            const uint32_t bhi = smem_addr(smem + PL::OFF_B1);
-            const uint32_t blo = bhi + PL::B1_BYTES;
-            int i = 0;
-#pragma unroll
-            for (int s = 0; s < PL::K1 / 16; ++s) {
-                const uint32_t oa = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
-                const uint32_t ob = (uint32_t)((s >> 2) * PL::NN1 * 128 + (s & 3) * 32);
-                const uint32_t d = d1 + (uint32_t)(h * PL::NN1);
-                tc::mma_f16(d, tc::desc_sw128(ahi + oa), tc::desc_sw128(bhi + ob), idesc, i++ > 0);
-                tc::mma_f16(d, tc::desc_sw128(alo + oa), tc::desc_sw128(bhi + ob), idesc, true);
-                if constexpr (PL::TERMS == 3) tc::mma_f16(d, tc::desc_sw128(ahi + oa), tc::desc_sw128(blo + ob), idesc, true);
-            }
-        }
-        tc::mma_commit(bars + 1);
-    };
-
-    auto issue_gemm3 = [&]() {
-        constexpr uint32_t idesc = tc::idesc_f16(128, PL::NN3, !PL::FP16);
-        const uint32_t ahi = smem_addr(smem + PL::OFF_A3);
-        const uint32_t alo = ahi + PL::A3_BYTES;
-        const uint32_t bhi = smem_addr(smem + PL::OFF_B3);
-        const uint32_t blo = bhi + PL::B3_BYTES;
-#pragma unroll
-        for (int s = 0; s < PL::K3 / 16; ++s) {
-            const uint32_t oa = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
-            const uint32_t ob = (uint32_t)((s >> 2) * PL::NN3 * 128 + (s & 3) * 32);
-            tc::mma_f16(d3, tc::desc_sw128(ahi + oa), tc::desc_sw128(bhi + ob), idesc, s > 0);
-            tc::mma_f16(d3, tc::desc_sw128(alo + oa), tc::desc_sw128(bhi + ob), idesc, true);
-            if constexpr (PL::TERMS == 3) tc::mma_f16(d3, tc::desc_sw128(ahi + oa), tc::desc_sw128(blo + ob), idesc, true);
-        }
-        tc::mma_commit(bars + 2);
-    };
-
-    // operand writes by every thread -> visible to the tensor core, then one thread issues
-    auto publish = [&]() {
-        fence_proxy_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-    };
-
-    // ---- twiddle + split: D1 -> A3.  Thread -> (chain h1, D1 lane m1, k2 range)
-    constexpr int K2W = N2 / WPQ1;
-    const int k2a = PL::HALVES == 2 ? 0 : (warp >> 2) * K2W;
-    auto twiddle_split = [&]() {
-        unsigned char *ahi = smem + PL::OFF_A3;
-        unsigned char *alo = ahi + PL::A3_BYTES;
-        const uint32_t taddr = d1 + (uint32_t)(h1 * PL::NN1) + ((uint32_t)(quarter * 32) << 16);
-#pragma unroll
-        for (int c = 0; c < K2W; c += 16) {         // 16 k2 = 32 columns per load
-            float v[32];
-            tc::tmem_ld32(taddr + (uint32_t)(2 * (k2a + c)), v);
-            tc::tmem_wait_ld();
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                const int k2 = k2a + c + i;
-                const float2 w = tw[k2 * N1 + n1];
-                const float2 y = cmul(make_float2(v[2 * i], v[2 * i + 1]), w);
-                uint32_t hw, lw;
-                split2<PL::FP16>(y.x, y.y, hw, lw);
-                const uint32_t off = tc::sw128_offset(128, N2 * row1 + k2, 2 * n1);
-                *reinterpret_cast<uint32_t *>(ahi + off) = hw;
-                *reinterpret_cast<uint32_t *>(alo + off) = lw;
-            }
-        }
-    };
-
-    // ---- epilogue: D3 lane m3 = N2 R + k2; this warp's half of the columns
-    const int m3 = quarter * 32 + lane;
-    const int row3 = m3 / N2, k2e = m3 % N2;
-    const int k1a = (warp >> 2) * PL::PIX;
-    const bool valid3 = yb + row3 < p.rows;
-    float minv[PL::PIX];
-    int mink[PL::PIX];
-#pragma unroll
-    for (int i = 0; i < PL::PIX; ++i) { minv[i] = __int_as_float(0x7f800000); mink[i] = 0; }
-    auto reduce = [&](int k, float inv_s2) {
-        const uint32_t taddr = d3 + (uint32_t)(2 * k1a) + ((uint32_t)(quarter * 32) << 16);
-#pragma unroll
-        for (int c = 0; c < PL::PIX; c += 16) {
-            float v[32];
-            tc::tmem_ld32(taddr + (uint32_t)(2 * c), v);
-            tc::tmem_wait_ld();
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                float i2 = fmaf(v[2 * i], v[2 * i], v[2 * i + 1] * v[2 * i + 1]);
-                if constexpr (PL::FP16) i2 *= inv_s2;
-                if (i2 < minv[c + i]) { minv[c + i] = i2; mink[c + i] = k; }
-            }
-        }
-    };
-
-    // A wait that gives up raises p.err; the CTA then stops after its next
-    // barrier (every thread reads the flag there), so a copy or an MMA that
-    // never completes costs one bounded wait per CTA, not one per slice.
     const volatile int *errv = p.err;
-    // The rows of a later slice are prefetched into L2 by the copy engine, so
-    // that the loads of load_split meet L2 rather than DRAM latency.
-    const uint32_t tile_bytes = (uint32_t)(min(PL::ROWS, p.rows - yb) * N * 8);
-    auto prefetch = [&](int b) {
-        if (t == 0 && b < b1) tc::prefetch_l2(p.t + ((size_t)b * p.rows + yb) * N, tile_bytes);
-    };
-    prefetch(b0 + 1);
-    uint32_t ph1 = 0, ph3 = 0;
-    mbar_wait(bars + 0, 0, p.err);                // tables in shared memory
-    load_split(b0);
-    float scale_cur = scale;
-    publish();
-    if (t == 0 && *errv == 0) issue_gemm1();
-    for (int b = b0; b < b1; ++b) {
-        mbar_wait(bars + 1, ph1, p.err);           // GEMM 1 of slice b done: D1 ready, A1 free
-        ph1 ^= 1u;
-        tc::fence_after_sync();
-        twiddle_split();
-        publish();
-        if (*errv != 0) break;                     // uniform: read by every thread after the barrier
-        if (t == 0) issue_gemm3();
-        prefetch(b + 2);
-        const float s_b = scale_cur;
-        if (b + 1 < b1) {
-            load_split(b + 1);
-            scale_cur = scale;
-            publish();
-            if (t == 0) issue_gemm1();
-        }
-        mbar_wait(bars + 2, ph3, p.err);           // GEMM 3 of slice b done: D3 ready, A3 free
-        ph3 ^= 1u;
-        tc::fence_after_sync();
-        reduce(p.k0 + b, 1.0f / (s_b * s_b));
-        tc::fence_before_sync();
-    }
-    if (valid3) {
-        unsigned long long *out = p.proj64 + (size_t)(yb + row3) * N;
+    mbar_wait(bars + 0, 0, p.err);                         // tables in shared memory
+
+    if (producer) {
+        // ---------------------------------------------------------- producers
+        const int pt = t - kTcConsumers, pw = pt >> 5;
+        const int m1 = pt;                                 // A1 row of every chain
+        const int r1 = m1 / N1, n1 = m1 % N1;
+        const uint32_t tile_bytes = (uint32_t)(min(PL::ROWS, p.rows - yb) * N * 8);
+        uint32_t ph1 = 0, phd = 0;
+        for (int b = b0; b < b1; ++b) {
+            if (b > b0) {                                  // GEMM 1 (b - 1) has read A1
+                mbar_wait(bars + 1, ph1, p.err);
+                ph1 ^= 1u;
+            }
+            if (pt == 0 && b + 2 < b1) tc::prefetch_l2(p.t + ((size_t)(b + 2) * p.rows + yb) * N, tile_bytes);
+#pragma unroll 1
+            for (int h = 0; h < PL::HALVES; ++h) {
+                const int row1 = h * PL::ROWS1 + r1;
+                const bool valid = yb + row1 < p.rows;
+                const float2 *src = p.t + ((size_t)b * p.rows + (valid ? yb + row1 : 0)) * N;
+                float2 v[N2];
 #pragma unroll
-        for (int i = 0; i < PL::PIX; ++i) atomicMin(out + k2e + N2 * (k1a + i), pack_min(minv[i], mink[i]));
+                for (int i = 0; i < N2; ++i) v[i] = valid ? __ldcs(src + n1 + N1 * i) : make_float2(0.f, 0.f);
+                if constexpr (PL::FP16) {
+                    // per-row power-of-two scale: the row's largest value at most 2^9
+                    float mx = 0.0f;
+#pragma unroll
+                    for (int i = 0; i < N2; ++i) mx = fmaxf(mx, fmaxf(fabsf(v[i].x), fabsf(v[i].y)));
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                    constexpr int WPR = N1 / 32;           // producer warps per row
+                    if (WPR > 1) {
+                        if (lane == 0) rmax[pw] = mx;
+                        asm volatile("bar.sync 1, %0;" ::"r"(kTcProducers) : "memory");
+                        mx = fmaxf(rmax[pw & ~1], rmax[pw | 1]);
+                        asm volatile("bar.sync 1, %0;" ::"r"(kTcProducers) : "memory");
+                    }
+                    int e = 0;
+                    frexpf(mx, &e);
+                    const float sc = mx > 0.0f ? ldexpf(1.0f, 9 - e) : 1.0f;
+                    if (n1 == 0) rscale[(b & 1) * PL::ROWS + row1] = sc;
+#pragma unroll
+                    for (int i = 0; i < N2; ++i) v[i] = make_float2(v[i].x * sc, v[i].y * sc);
+                }
+                unsigned char *ahi = smem + PL::OFF_A1 + (2 * h) * PL::A1_BYTES;
+                unsigned char *alo = ahi + PL::A1_BYTES;
+#pragma unroll
+                for (int i = 0; i < N2; i += 4) {
+                    uint4 hv, lv;
+                    split2<PL::FP16>(v[i].x, v[i].y, hv.x, lv.x);
+                    split2<PL::FP16>(v[i + 1].x, v[i + 1].y, hv.y, lv.y);
+                    split2<PL::FP16>(v[i + 2].x, v[i + 2].y, hv.z, lv.z);
+                    split2<PL::FP16>(v[i + 3].x, v[i + 3].y, hv.w, lv.w);
+                    const uint32_t off = tc::sw128_offset(128, m1, 2 * i);
+                    *reinterpret_cast<uint4 *>(ahi + off) = hv;
+                    *reinterpret_cast<uint4 *>(alo + off) = lv;
+                }
+            }
+            if constexpr (PL::FP16) mbar_arrive(bars + 4 + (b & 1));   // this tile's row scales are written
+            fence_proxy_async_smem();
+            // every producer has written A1; stop together if any wait anywhere gave up
+            const bool stop = bar_sync_or(1, kTcProducers, *errv != 0);
+            if (stop) break;
+            if (pt == 0) {
+                if (b > b0) {                              // the consumers have read D1 (b - 1)
+                    mbar_wait(bars + 3, phd, p.err);
+                    phd ^= 1u;
+                }
+                tc::fence_after_sync();
+                constexpr uint32_t idesc = tc::idesc_f16(128, PL::NN1, !PL::FP16);
+#pragma unroll
+                for (int h = 0; h < PL::HALVES; ++h) {
+                    const uint32_t ahi = smem_addr(smem + PL::OFF_A1 + (2 * h) * PL::A1_BYTES);
+                    const uint32_t alo = ahi + PL::A1_BYTES;
+                    const uint32_t bhi = smem_addr(smem + PL::OFF_B1);
+                    const uint32_t blo = bhi + PL::B1_BYTES;
+                    const uint32_t d = d1 + (uint32_t)(h * PL::NN1);
+#pragma unroll
+                    for (int s = 0; s < PL::K1 / 16; ++s) {
+                        const uint32_t oa = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
+                        const uint32_t ob = (uint32_t)((s >> 2) * PL::NN1 * 128 + (s & 3) * 32);
+                        tc::mma_f16(d, tc::desc_sw128(ahi + oa), tc::desc_sw128(bhi + ob), idesc, s > 0);
+                        tc::mma_f16(d, tc::desc_sw128(alo + oa), tc::desc_sw128(bhi + ob), idesc, true);
+                        if constexpr (PL::TERMS == 3)
+                            tc::mma_f16(d, tc::desc_sw128(ahi + oa), tc::desc_sw128(blo + ob), idesc, true);
+                    }
+                }
+                tc::mma_commit(bars + 1);
+            }
+        }
+    } else {
+        // ---------------------------------------------------------- consumers
+        const int quarter = warp & 3;                      // tensor-memory lane quarter
+        // twiddle + split: D1 lane m of chain h -> A3 rows N2 R + k2, K 2 n1 + c
+        constexpr int WPQ1 = 2 / PL::HALVES;
+        const int h1 = PL::HALVES == 2 ? (warp >> 2) : 0;
+        const int m1 = quarter * 32 + lane;
+        const int r1 = m1 / N1, n1 = m1 % N1;
+        const int row1 = h1 * PL::ROWS1 + r1;
+        constexpr int K2W = N2 / WPQ1;
+        const int k2a = PL::HALVES == 2 ? 0 : (warp >> 2) * K2W;
+        // reduction: D3 lane m3 = N2 R + k2, this warp's half of the columns
+        const int m3 = quarter * 32 + lane;
+        const int row3 = m3 / N2, k2e = m3 % N2;
+        const int k1a = (warp >> 2) * PL::PIX;
+        const bool valid3 = yb + row3 < p.rows;
+        float minv[PL::PIX];
+        int mink[PL::PIX];
+#pragma unroll
+        for (int i = 0; i < PL::PIX; ++i) { minv[i] = __int_as_float(0x7f800000); mink[i] = 0; }
+        uint32_t ph1 = 0, ph3 = 0, phs0 = 0, phs1 = 0;
+        for (int b = b0; b < b1; ++b) {
+            mbar_wait(bars + 1, ph1, p.err);               // GEMM 1 (b) done: D1 ready
+            ph1 ^= 1u;
+            float inv_s2 = 1.0f;
+            if constexpr (PL::FP16) {
+                uint32_t &ps = (b & 1) ? phs1 : phs0;
+                mbar_wait(bars + 4 + (b & 1), ps, p.err);
+                ps ^= 1u;
+                const float sc = rscale[(b & 1) * PL::ROWS + row3];
+                inv_s2 = 1.0f / (sc * sc);
+            }
+            tc::fence_after_sync();
+            {
+                unsigned char *ahi = smem + PL::OFF_A3;
+                unsigned char *alo = ahi + PL::A3_BYTES;
+                const uint32_t taddr = d1 + (uint32_t)(h1 * PL::NN1) + ((uint32_t)(quarter * 32) << 16);
+#pragma unroll
+                for (int c = 0; c < K2W; c += 16) {        // 16 k2 = 32 columns per load
+                    float v[32];
+                    tc::tmem_ld32(taddr + (uint32_t)(2 * (k2a + c)), v);
+                    tc::tmem_wait_ld();
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int k2 = k2a + c + i;
+                        const float2 w = tw[k2 * N1 + n1];
+                        const float2 y = cmul(make_float2(v[2 * i], v[2 * i + 1]), w);
+                        uint32_t hw, lw;
+                        split2<PL::FP16>(y.x, y.y, hw, lw);
+                        const uint32_t off = tc::sw128_offset(128, N2 * row1 + k2, 2 * n1);
+                        *reinterpret_cast<uint32_t *>(ahi + off) = hw;
+                        *reinterpret_cast<uint32_t *>(alo + off) = lw;
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            mbar_arrive(bars + 3);                         // D1 (b) read: GEMM 1 (b + 1) may write it
+            fence_proxy_async_smem();
+            const bool stop = bar_sync_or(2, kTcConsumers, *errv != 0);   // a uniform decision
+            tc::fence_after_sync();
+            if (stop) break;
+            if (t == 0) {
+                constexpr uint32_t idesc = tc::idesc_f16(128, PL::NN3, !PL::FP16);
+                const uint32_t ahi = smem_addr(smem + PL::OFF_A3);
+                const uint32_t alo = ahi + PL::A3_BYTES;
+                const uint32_t bhi = smem_addr(smem + PL::OFF_B3);
+                const uint32_t blo = bhi + PL::B3_BYTES;
+#pragma unroll
+                for (int s = 0; s < PL::K3 / 16; ++s) {
+                    const uint32_t oa = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
+                    const uint32_t ob = (uint32_t)((s >> 2) * PL::NN3 * 128 + (s & 3) * 32);
+                    tc::mma_f16(d3, tc::desc_sw128(ahi + oa), tc::desc_sw128(bhi + ob), idesc, s > 0);
+                    tc::mma_f16(d3, tc::desc_sw128(alo + oa), tc::desc_sw128(bhi + ob), idesc, true);
+                    if constexpr (PL::TERMS == 3)
+                        tc::mma_f16(d3, tc::desc_sw128(ahi + oa), tc::desc_sw128(blo + ob), idesc, true);
+                }
+                tc::mma_commit(bars + 2);
+            }
+            mbar_wait(bars + 2, ph3, p.err);               // GEMM 3 (b) done: D3 ready, A3 free
+            ph3 ^= 1u;
+            tc::fence_after_sync();
+            const int k = p.k0 + b;
+            const uint32_t taddr = d3 + (uint32_t)(2 * k1a) + ((uint32_t)(quarter * 32) << 16);
+#pragma unroll
+            for (int c = 0; c < PL::PIX; c += 16) {
+                float v[32];
+                tc::tmem_ld32(taddr + (uint32_t)(2 * c), v);
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    float i2 = fmaf(v[2 * i], v[2 * i], v[2 * i + 1] * v[2 * i + 1]);
+                    if constexpr (PL::FP16) i2 *= inv_s2;
+                    if (i2 < minv[c + i]) { minv[c + i] = i2; mink[c + i] = k; }
+                }
+            }
+            tc::fence_before_sync();
+        }
+        if (valid3) {
+            unsigned long long *out = p.proj64 + (size_t)(yb + row3) * N;
+#pragma unroll
+            for (int i = 0; i < PL::PIX; ++i) atomicMin(out + k2e + N2 * (k1a + i), pack_min(minv[i], mink[i]));
+        }
     }
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, PL::TMEM_COLS);

@@ -81,14 +81,15 @@ def test_requests_wait_for_budget_then_complete(ph, cuda):
     """Admission against the HBM budget: with room for one request's scratch, the
     later ones queue at submission and run as the earlier ones finish; every
     result equals the single call."""
-    n, slices = 1024, 64
+    n, slices = 1024, 512       # ~3 ms each: the later submissions arrive while the first runs
     block = _block_bytes(ph, cuda, n, slices)
     srv = ph.Server(max_shape=(n, n), max_slices=slices, lanes=4, budget_bytes=int(block * 1.5))
     rng = np.random.default_rng(3)
+    holos = [to_dev(rng.uniform(0.1, 1.0, (n, n)).astype(np.float32), cuda) for _ in range(3)]
+    outs = [(torch.empty_like(h), torch.empty(h.shape, dtype=torch.int32, device=cuda)) for h in holos]
+    torch.cuda.synchronize()
     reqs = []
-    for i in range(3):
-        holo = to_dev(rng.uniform(0.1, 1.0, (n, n)).astype(np.float32), cuda)
-        proj, arg = torch.empty_like(holo), torch.empty(holo.shape, dtype=torch.int32, device=cuda)
+    for i, (holo, (proj, arg)) in enumerate(zip(holos, outs)):
         reqs.append((srv.submit(holo, proj, slices, 1000.0 + 100 * i, 200.0, argmin=arg), holo, proj, arg, i))
     st = srv.stats()
     assert st["waited"] == 2 and st["running"] + st["queued"] <= 3
