@@ -85,7 +85,8 @@ enum {
     PH_FORM_FP32 = 0,     /* radix-16 Stockham FFT on the CUDA cores, FP32 */
     PH_FORM_BF16X3 = 1,   /* BF16 pairs, products hi.hi + lo.hi + hi.lo */
     PH_FORM_FP16X3 = 2,   /* FP16 pairs (tiles scaled by powers of two), three products */
-    PH_FORM_FP16X2 = 3    /* FP16 data pairs, DFT matrix in one FP16 word: hi.hi + lo.hi */
+    PH_FORM_FP16X2 = 3,   /* FP16 data pairs, DFT matrix in one FP16 word: hi.hi + lo.hi */
+    PH_FORM_TUNED = 4     /* the form ph_autotune chose for the shape (FP32 where it chose none) */
 };
 
 /* ---- diagnostics ----------------------------------------------------------- */
@@ -120,6 +121,21 @@ PH_API int64_t ph_kernel_launches(const ph_ctx *ctx);
  * name into buf (NUL-terminated, truncated to cap), then clears the records.
  * Synchronises on the recorded events.  Returns the bytes needed. */
 PH_API int64_t ph_profile_report(ph_ctx *ctx, char *buf, int64_t cap);
+
+/* The autotuner (no reference counterpart): times the reconstruction of an
+ * n_fast x n_slow x slices projection once per candidate -- slices per pass
+ * CTA (the built-in rule, 16, 32, 64), the batch of slice intermediates (the
+ * built-in rule, 64 slices) and, with allow_forms, the split-precision row-pass
+ * forms -- on synthetic inputs, and keeps the fastest for the shape in the
+ * context: every later reconstruction of that shape (single calls, batch
+ * plans, servers) uses its slice group and batch, and its form under
+ * PH_OPT_FORM = PH_FORM_TUNED.  With cache_path, the choice is read from and
+ * written to a JSON file keyed by device name and shape (a shape already in
+ * the file for the same slice count is not timed again).  choice (nullable,
+ * int32[3]) = {form, group cap, batch slices} (0 = built-in rule); *ms_out
+ * (nullable) = its time per reconstruction.  Synchronises; not inside a capture. */
+PH_API int32_t ph_autotune(ph_ctx *ctx, int32_t n_fast, int32_t n_slow, int32_t slices, int32_t allow_forms,
+                           const char *cache_path, int32_t *choice, double *ms_out, void *stream);
 
 /* ---- transfer functions ---------------------------------------------------- */
 

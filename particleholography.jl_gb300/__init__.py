@@ -9,7 +9,7 @@ The directory name is not a Python identifier; load the package with
 ``__graft_entry__.load_package()`` (it registers it as ``ph_gb300``).
 """
 from . import _lib
-from .batch import ReconBatch
+from .batch import ReconBatch, autotune
 from .detection import (cu_get_reconst_binary_vol, cu_reconst_subvolumes, particle_coordinates,
                         slice_bounding_boxes)
 from .serve import Server

@@ -34,7 +34,7 @@ PH_OPT_PROFILE = 4
 PH_OPT_FORM = 5
 
 # forms of the projection's row pass
-PH_FORM_FP32, PH_FORM_BF16X3, PH_FORM_FP16X3, PH_FORM_FP16X2 = range(4)
+PH_FORM_FP32, PH_FORM_BF16X3, PH_FORM_FP16X3, PH_FORM_FP16X2, PH_FORM_TUNED = range(5)
 
 # identity of the packed-minimum merge (ph_reconst_xyproj_range)
 PH_PACKED_EMPTY = 0x7FFFFFFFFFFFFFFF
@@ -66,6 +66,7 @@ SIGNATURES = {
     "ph_asm_prop": (_i32, [_vp, _vp, _vp, _vp, _f64, _i32, _i32, _f64, _vp]),
     "ph_reconst_xyproj": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),
     "ph_tc_selftest": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp]),
+    "ph_autotune": (_i32, [_vp, _i32, _i32, _i32, _i32, ctypes.c_char_p, _vp, ctypes.POINTER(_f64), _vp]),
     "ph_reconst_xyproj_range": (_i32, [_vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
     "ph_unpack_projection": (_i32, [_vp, _vp, _vp, _vp, _i32, _i32, _vp]),
     "ph_reconst_xyproj_lpf": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _i32, _vp]),

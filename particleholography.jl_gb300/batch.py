@@ -83,3 +83,22 @@ class ReconBatch:
             self.close()
         except Exception:
             pass
+
+
+def autotune(n_fast: int, n_slow: int, slices: int, allow_forms: bool = False, cache: str | None = None,
+             device: int | None = None) -> dict:
+    """The library's autotuner (``ph_autotune``) for one shape: times the
+    projection's knobs once (slices per CTA, batch of intermediates and, with
+    ``allow_forms``, the split-precision row-pass forms) and keeps the fastest
+    in the device's context, so later reconstructions of the shape -- single
+    calls, batch plans, servers -- use it.  With ``cache`` (a JSON path) the
+    choice is read from / written to the file, keyed by device name and shape.
+    Returns ``{"form", "group_cap", "batch_slices", "ms"}``."""
+    dev = torch.cuda.current_device() if device is None else device
+    ctx = _lib.default_context(dev)
+    choice = (ctypes.c_int32 * 3)()
+    ms = ctypes.c_double()
+    s = torch.cuda.current_stream(dev).cuda_stream
+    ctx.call("ph_autotune", int(n_fast), int(n_slow), int(slices), 1 if allow_forms else 0,
+             cache.encode() if cache is not None else None, ctypes.addressof(choice), ctypes.byref(ms), s)
+    return {"form": int(choice[0]), "group_cap": int(choice[1]), "batch_slices": int(choice[2]), "ms": ms.value}

@@ -761,8 +761,30 @@ int issue_spectrum(ph_ctx *ctx, const float2 *wf, const float2 *hf, const float2
 constexpr size_t kBatchBytes = size_t(16) << 30;
 constexpr size_t kLaneBatchBytes = size_t(2) << 30;
 
+// The autotuner's knobs for a transform shape, or null.
+const ph_tuning *tuning_of(const ph_ctx *ctx, int nx, int ny) {
+    auto it = ctx->tuned.find({nx, ny});
+    return it == ctx->tuned.end() ? nullptr : &it->second;
+}
+
+// The form of the projection's row pass for this shape: the caller's choice,
+// or under PH_FORM_TUNED the tuner's (FP32 where it chose none or the length
+// has no tensor-core plan).
+int effective_form(const ph_ctx *ctx, int nx, int ny) {
+    int f = (int)ctx->opt_form;
+    if (f == PH_FORM_TUNED) {
+        const ph_tuning *tu = tuning_of(ctx, nx, ny);
+        f = tu ? tu->form : PH_FORM_FP32;
+    }
+    return (f != PH_FORM_FP32 && recon_b_tc_supported(nx, f)) ? f : PH_FORM_FP32;
+}
+
 int slice_batch(ph_ctx *ctx, int nx, int ny, int slices, size_t target = kBatchBytes) {
     if (ctx->opt_slice_batch > 0) return (int)std::min<int64_t>(ctx->opt_slice_batch, slices);
+    if (const ph_tuning *tu = tuning_of(ctx, nx, ny); tu && tu->batch_slices > 0) {
+        const size_t fit = std::max<size_t>(1, target / ((size_t)nx * ny * sizeof(float2)));
+        return (int)std::min<size_t>({(size_t)tu->batch_slices, fit, (size_t)std::max(slices, 1)});
+    }
     const size_t slice_bytes = (size_t)nx * ny * sizeof(float2);
     if (ctx->budget) target = std::min(target, ctx->budget / 2);
     // clamped in size_t: a tiny slice would overflow an int count
@@ -830,17 +852,18 @@ int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void 
     auto *p64 = packed != nullptr ? packed : at<unsigned long long>(ctx, L.p64);
     float2 *t = at<float2>(ctx, L.t);
     const bool want_proj = (kind == RK_PROJ) || proj != nullptr || argmin != nullptr;
-    if (kind == RK_PROJ && ctx->opt_form != PH_FORM_FP32 && recon_b_tc_supported(nx, (int)ctx->opt_form)) {
+    if (kind == RK_PROJ && effective_form(ctx, nx, ny) != PH_FORM_FP32) {
         const unsigned char *tab = nullptr;
-        PH_TRY(get_tc_table(ctx, nx, (int)ctx->opt_form, s, &tab));
+        PH_TRY(get_tc_table(ctx, nx, effective_form(ctx, nx, ny), s, &tab));
     }
+    const ph_tuning *tu = tuning_of(ctx, nx, ny);
     char key[512];
     uint32_t thr_bits = 0;
     memcpy(&thr_bits, &threshold, sizeof thr_bits);
     snprintf(key, sizeof key, "recon|%d|%d|%d|%d|%d|%d|%p|%p|%p|%p|%p|%p|%p|%d|%p|%08x|%p|%d|%d|%d", (int)kind, nin_x,
              nin_y, slices, L.batch, vol_dtype, (void *)proj, (void *)argmin, vol, (const void *)wf, (const void *)hf,
              (const void *)hdz, ctx->scratch, (int)ctx->opt_loop_limit, (const void *)lpf, thr_bits, (void *)packed,
-             (int)accumulate, first, (int)ctx->opt_form);
+             (int)accumulate, first, effective_form(ctx, nx, ny) * 1000 + (tu ? tu->group_cap : 0));
     return run_graph(ctx, s, key, [&](cudaStream_t s) -> int {
         PH_TRY(issue_spectrum(ctx, wf, hf, hdz, nx, ny, padded, nin_x, nin_y, at<float2>(ctx, L.a1), state, tw_x,
                               tw_y, at<double>(ctx, L.acc), at<float2>(ctx, L.mean), s, nullptr, lpf));
@@ -866,7 +889,8 @@ int reconstruct(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void 
 // sin/cos per value) as long as pass A keeps at least 16 waves of CTAs: 1.2 %
 // faster per 2048^2 x 512 frame.  (A 64 cap without the wave condition made
 // 1024^2 x 256 frames 7 % slower: 5 waves, the last one nearly empty.)
-int recon_group(int nbatch, int nx_rows_a, bool chain) {
+int recon_group(int nbatch, int nx_rows_a, bool chain, int cap_override = 0) {
+    if (cap_override > 0) return std::max(1, std::min(cap_override, nbatch));
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
@@ -892,7 +916,8 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
     const int row_blocks_a = (nx + recon_a_rows(ny) - 1) / recon_a_rows(ny);
     for (int k0 = first; k0 < first + slices; k0 += L.batch) {
         const int nb = std::min(L.batch, first + slices - k0);
-        const int group = recon_group(nb, row_blocks_a, recon_a_chain(ny));
+        const ph_tuning *tu = tuning_of(ctx, nx, ny);
+        const int group = recon_group(nb, row_blocks_a, recon_a_chain(ny), tu ? tu->group_cap : 0);
         ReconA a{};
         a.state = state;
         a.t = t;
@@ -905,12 +930,13 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
         a.group = group;
         a.err = static_cast<int *>(ctx->small);
         PH_TRY(pass(ctx, s, "recon_a",[&] { return launch_recon_a(ny, a, nb, s); }));
-        if (kind == RK_PROJ && ctx->opt_form != PH_FORM_FP32 && recon_b_tc_supported(nx, (int)ctx->opt_form)) {
+        if (kind == RK_PROJ && effective_form(ctx, nx, ny) != PH_FORM_FP32) {
+            const int form = effective_form(ctx, nx, ny);
             ReconBTc b{};
-            PH_TRY(get_tc_table(ctx, nx, (int)ctx->opt_form, s, &b.table));
+            PH_TRY(get_tc_table(ctx, nx, form, s, &b.table));
             b.t = t; b.proj64 = p64; b.rows = ny_out; b.k0 = k0; b.nbatch = nb; b.group = group;
             b.err = static_cast<int *>(ctx->small);
-            PH_TRY(pass(ctx, s, "recon_b_tc", [&] { return launch_recon_b_tc(nx, (int)ctx->opt_form, b, s); }));
+            PH_TRY(pass(ctx, s, "recon_b_tc", [&] { return launch_recon_b_tc(nx, form, b, s); }));
         } else if (kind == RK_PROJ) {
             ReconB<EPI_PROJ> b{};
             b.t = t; b.tw = tw_x; b.proj64 = p64; b.rows = ny_out; b.nx_out = nx_out; b.x0 = 0;
@@ -1165,7 +1191,7 @@ int32_t ph_set_option(ph_ctx *ctx, int32_t option, int64_t value) {
             return PH_OK;
         case PH_OPT_PROFILE: ctx->opt_profile = value; return PH_OK;
         case PH_OPT_FORM:
-            if (value < PH_FORM_FP32 || value > PH_FORM_FP16X2) break;
+            if (value < PH_FORM_FP32 || value > PH_FORM_TUNED) break;
             ctx->opt_form = value;
             return PH_OK;
     }
@@ -1519,6 +1545,254 @@ int32_t ph_reconst_xyproj(ph_ctx *ctx, float *proj, int32_t *argmin, const void 
     PH_TRY(reconstruct(ctx, RK_PROJ, proj, argmin, nullptr, PH_F32, static_cast<const float2 *>(wf),
                        static_cast<const float2 *>(tf_front), static_cast<const float2 *>(tf_dz), n_fast, n_slow,
                        slices, s));
+    PH_LEAVE(ctx);
+}
+
+// ---- autotuner: the reconstruction knobs per (n_fast, n_slow, device), timed once, cached as JSON
+namespace {
+
+// The cache file: {"<device>": {"<n_fast>x<n_slow>": {"slices": S, "form": F,
+// "group_cap": G, "batch_slices": B, "ms": T}, ...}, ...}.  A small reader for
+// exactly this shape (objects, strings, numbers).
+struct JsonTune {
+    std::map<std::string, std::map<std::string, std::map<std::string, double>>> dev;
+};
+
+void skip_ws(const std::string &t, size_t &i) {
+    while (i < t.size() && (t[i] == ' ' || t[i] == '\n' || t[i] == '\r' || t[i] == '\t' || t[i] == ',')) ++i;
+}
+bool read_str(const std::string &t, size_t &i, std::string &out) {
+    skip_ws(t, i);
+    if (i >= t.size() || t[i] != '"') return false;
+    const size_t j = t.find('"', i + 1);
+    if (j == std::string::npos) return false;
+    out = t.substr(i + 1, j - i - 1);
+    i = j + 1;
+    skip_ws(t, i);
+    if (i >= t.size() || t[i] != ':') return false;
+    ++i;
+    return true;
+}
+bool expect(const std::string &t, size_t &i, char c) {
+    skip_ws(t, i);
+    if (i >= t.size() || t[i] != c) return false;
+    ++i;
+    return true;
+}
+bool peek(const std::string &t, size_t &i, char c) {
+    skip_ws(t, i);
+    return i < t.size() && t[i] == c;
+}
+
+bool parse_tune(const std::string &t, JsonTune &out) {
+    size_t i = 0;
+    if (!expect(t, i, '{')) return false;
+    while (!peek(t, i, '}')) {
+        std::string dname;
+        if (!read_str(t, i, dname) || !expect(t, i, '{')) return false;
+        while (!peek(t, i, '}')) {
+            std::string shape;
+            if (!read_str(t, i, shape) || !expect(t, i, '{')) return false;
+            while (!peek(t, i, '}')) {
+                std::string key;
+                if (!read_str(t, i, key)) return false;
+                skip_ws(t, i);
+                char *end = nullptr;
+                const double v = strtod(t.c_str() + i, &end);
+                if (end == t.c_str() + i) return false;
+                i = end - t.c_str();
+                out.dev[dname][shape][key] = v;
+            }
+            ++i;
+        }
+        ++i;
+    }
+    return true;
+}
+
+std::string dump_tune(const JsonTune &j) {
+    std::string o = "{\n";
+    bool first_d = true;
+    for (auto &d : j.dev) {
+        o += (first_d ? "" : ",\n");
+        first_d = false;
+        o += " \"" + d.first + "\": {\n";
+        bool first_s = true;
+        for (auto &sh : d.second) {
+            o += (first_s ? "" : ",\n");
+            first_s = false;
+            o += "  \"" + sh.first + "\": {";
+            bool first_k = true;
+            for (auto &kv : sh.second) {
+                char num[64];
+                snprintf(num, sizeof num, "%.6g", kv.second);
+                o += (first_k ? "" : ", ");
+                first_k = false;
+                o += "\"" + kv.first + "\": " + num;
+            }
+            o += "}";
+        }
+        o += "\n }";
+    }
+    return o + "\n}\n";
+}
+
+std::string read_file(const char *path) {
+    std::string t;
+    if (FILE *f = fopen(path, "rb")) {
+        char buf[4096];
+        size_t n;
+        while ((n = fread(buf, 1, sizeof buf, f)) > 0) t.append(buf, n);
+        fclose(f);
+    }
+    return t;
+}
+
+}  // namespace
+
+int32_t ph_autotune(ph_ctx *ctx, int32_t n_fast, int32_t n_slow, int32_t slices, int32_t allow_forms,
+                    const char *cache_path, int32_t *choice, double *ms_out, void *stream) {
+    PH_ENTER(ctx, stream);
+    PH_TRY(check_len(ctx, n_fast, n_slow));
+    if (slices < 1) { set_err(ctx, "slices must be >= 1. Got %d.", slices); return PH_ERR_SIZE; }
+    if (capturing(s)) { set_err(ctx, "ph_autotune times launches and cannot run inside a stream capture"); return PH_ERR_INVALID; }
+    cudaDeviceProp prop{};
+    PH_CUDA(cudaGetDeviceProperties(&prop, ctx->device), "cudaGetDeviceProperties");
+    std::string dname = prop.name;
+    for (auto &c : dname) if (c == '"' || c == '\\') c = '_';
+    char shape[64];
+    snprintf(shape, sizeof shape, "%dx%d", n_fast, n_slow);
+    JsonTune cache;
+    if (cache_path != nullptr) {
+        const std::string text = read_file(cache_path);
+        if (!text.empty() && !parse_tune(text, cache)) cache.dev.clear();   // unreadable: retune and rewrite
+    }
+    auto report = [&](const ph_tuning &tu) {
+        if (choice) { choice[0] = tu.form; choice[1] = tu.group_cap; choice[2] = tu.batch_slices; }
+        if (ms_out) *ms_out = tu.ms;
+    };
+    auto dit = cache.dev.find(dname);
+    if (dit != cache.dev.end()) {
+        auto sit = dit->second.find(shape);
+        if (sit != dit->second.end() && (int)sit->second["slices"] == slices &&
+            (allow_forms || (int)sit->second["form"] == PH_FORM_FP32)) {
+            ph_tuning tu;
+            tu.form = (int)sit->second["form"];
+            tu.group_cap = (int)sit->second["group_cap"];
+            tu.batch_slices = (int)sit->second["batch_slices"];
+            tu.slices = slices;
+            tu.ms = sit->second["ms"];
+            ctx->tuned[{n_fast, n_slow}] = tu;
+            report(tu);
+            PH_LEAVE(ctx);
+        }
+    }
+    // timing inputs: unit-modulus transfer functions of the reference's form, and one as the wavefront
+    const size_t n = (size_t)n_fast * n_slow;
+    float2 *buf = nullptr;
+    float *dsqr = nullptr, *proj = nullptr;
+    int32_t *arg = nullptr;
+    PH_CUDA(cudaMalloc(&buf, 3 * n * sizeof(float2)), "cudaMalloc(tuning inputs)");
+    auto cleanup = [&]() {
+        cudaFree(buf);
+        if (dsqr) cudaFree(dsqr);
+        if (proj) cudaFree(proj);
+        if (arg) cudaFree(arg);
+    };
+    if (cudaMalloc(&dsqr, n * sizeof(float)) != cudaSuccess || cudaMalloc(&proj, n * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&arg, n * sizeof(int32_t)) != cudaSuccess) {
+        cleanup();
+        return cuda_status(ctx, cudaGetLastError(), "cudaMalloc(tuning outputs)");
+    }
+    float2 *wf = buf, *hf = buf + n, *hdz = buf + 2 * n;
+    dim3 b2(32, 8);
+    k_transfer_sqrt<<<grid2d(n_fast, n_slow, b2), b2, 0, s>>>(dsqr, n_fast, n_slow, 0.6328, 10.0);
+    k_transfer<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(wf, dsqr, n, (2.0 * M_PI * 3000.0) / 0.6328);
+    k_transfer<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(hf, dsqr, n, (2.0 * M_PI * -1000.0) / 0.6328);
+    k_transfer<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(hdz, dsqr, n, (2.0 * M_PI * -200.0) / 0.6328);
+    if (cudaGetLastError() != cudaSuccess) { cleanup(); return cuda_status(ctx, cudaErrorLaunchFailure, "tuning inputs"); }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int64_t saved_graphs = ctx->opt_use_graphs, saved_form = ctx->opt_form;
+    const auto saved_entry = ctx->tuned.find({n_fast, n_slow});
+    const bool had_entry = saved_entry != ctx->tuned.end();
+    const ph_tuning saved_tu = had_entry ? saved_entry->second : ph_tuning{};
+    ctx->opt_use_graphs = 0;
+    ctx->opt_form = PH_FORM_TUNED;
+    // candidates: slices per CTA, batch of intermediates (all / 64 slices), row-pass form
+    std::vector<int> forms = {PH_FORM_FP32};
+    if (allow_forms)
+        for (int f : {PH_FORM_BF16X3, PH_FORM_FP16X3})
+            if (recon_b_tc_supported(n_fast, f)) forms.push_back(f);
+    ph_tuning best;
+    best.ms = 1e300;
+    int st = PH_OK;
+    for (int form : forms) {
+        for (int cap : {0, 16, 32, 64}) {
+            for (int bs : {0, 64}) {
+                if (bs > 0 && bs >= slices) continue;
+                ph_tuning tu;
+                tu.form = form;
+                tu.group_cap = cap;
+                tu.batch_slices = bs;
+                tu.slices = slices;
+                ctx->tuned[{n_fast, n_slow}] = tu;
+                float best_ms = 1e30f;
+                for (int rep = 0; rep < 3 && st == PH_OK; ++rep) {   // the first run also builds the tables
+                    cudaEventRecord(e0, s);
+                    st = reconstruct(ctx, RK_PROJ, proj, arg, nullptr, PH_F32, wf, hf, hdz, n_fast, n_slow, slices, s);
+                    cudaEventRecord(e1, s);
+                    if (st != PH_OK) break;
+                    if (cudaEventSynchronize(e1) != cudaSuccess) { st = PH_ERR_CUDA; break; }
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (rep > 0) best_ms = std::min(best_ms, ms);
+                }
+                if (st != PH_OK) break;
+                if (best_ms < best.ms) {
+                    best = tu;
+                    best.ms = best_ms;
+                }
+            }
+            if (st != PH_OK) break;
+        }
+        if (st != PH_OK) break;
+    }
+    ctx->opt_use_graphs = saved_graphs;
+    ctx->opt_form = saved_form;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cleanup();
+    if (st != PH_OK) {
+        if (had_entry) ctx->tuned[{n_fast, n_slow}] = saved_tu;
+        else ctx->tuned.erase({n_fast, n_slow});
+        return st;
+    }
+    ctx->tuned[{n_fast, n_slow}] = best;
+    report(best);
+    if (cache_path != nullptr) {
+        auto &e = cache.dev[dname][shape];
+        e.clear();
+        e["slices"] = slices;
+        e["form"] = best.form;
+        e["group_cap"] = best.group_cap;
+        e["batch_slices"] = best.batch_slices;
+        e["ms"] = best.ms;
+        const std::string tmp = std::string(cache_path) + ".tmp";
+        FILE *f = fopen(tmp.c_str(), "wb");
+        const std::string text = dump_tune(cache);
+        if (f == nullptr || fwrite(text.data(), 1, text.size(), f) != text.size()) {
+            if (f) fclose(f);
+            set_err(ctx, "could not write the tuning cache %s", cache_path);
+            return PH_ERR_INVALID;
+        }
+        fclose(f);
+        if (rename(tmp.c_str(), cache_path) != 0) {
+            set_err(ctx, "could not replace the tuning cache %s", cache_path);
+            return PH_ERR_INVALID;
+        }
+    }
     PH_LEAVE(ctx);
 }
 

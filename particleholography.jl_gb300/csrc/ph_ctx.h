@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cstdint>
 #include <list>
+#include <map>
 #include <mutex>
 #include <string>
 #include <unordered_map>
@@ -16,6 +17,15 @@ struct ph_graph_entry {
     std::string key;
     cudaGraphExec_t exec = nullptr;
     int64_t kernels = 0;   // kernels launched by one replay
+};
+
+// Reconstruction knobs the autotuner chose for one (n_fast, n_slow).
+struct ph_tuning {
+    int form = 0;           // PH_FORM_* of the projection's row pass (used under PH_FORM_TUNED)
+    int group_cap = 0;      // slices per pass A / pass B CTA at most (0 = the built-in rule)
+    int batch_slices = 0;   // slices per batch of intermediates (0 = the built-in rule)
+    int slices = 0;         // slices of the workload it was timed on
+    double ms = 0.0;        // its time per reconstruction
 };
 
 struct ph_prof_record {
@@ -62,6 +72,7 @@ struct ph_ctx {
     int64_t opt_loop_limit = int64_t(1) << 20;
     int64_t opt_profile = 0;
     int64_t opt_form = 0;           // PH_FORM_*: arithmetic of the projection's row pass
+    std::map<std::pair<int, int>, ph_tuning> tuned;   // (n_fast, n_slow) -> autotuner's choice
 
     // profiler: pending event pairs and a pool of spare events
     std::vector<ph_prof_record> prof;

@@ -79,3 +79,43 @@ def test_batch_rejects_bad_items(ph, cuda):
     mismatched = dict(good, transfer_dz=torch.zeros((32, 64), dtype=torch.complex64, device=good["hologram"].device))
     with pytest.raises(AssertionError):
         ph.ReconBatch([mismatched])
+
+
+def test_autotune_choice_cached_and_used(ph, cuda, tmp_path):
+    """The autotuner times the knobs of a shape once, writes its choice to the
+    JSON cache keyed by device and shape, reads it back without timing again,
+    and reconstructions under the chosen knobs still match the oracle."""
+    import json
+    from oracle import ref_semantics as ref
+    from phtest import ARGMIN_AGREE, REL_L2, rel_l2, to_dev, to_np
+    from ph_gb300 import _lib
+    cache = tmp_path / "tune.json"
+    n, slices = 256, 96
+    first = ph.autotune(n, n, slices, allow_forms=False, cache=str(cache))
+    assert first["ms"] > 0 and first["form"] == 0 and first["group_cap"] in (0, 16, 32, 64)
+    data = json.loads(cache.read_text())
+    (dev, shapes), = data.items()
+    assert "GB300" in dev and shapes[f"{n}x{n}"]["slices"] == slices
+    again = ph.autotune(n, n, slices, cache=str(cache))
+    assert again == first                                  # read back, not timed again
+    rng = np.random.default_rng(5)
+    holo = rng.uniform(0.1, 1.0, (n, n)).astype(np.float32)
+    d = ref.transfer_sqrt_arr(n, 0.6328, 10.0)
+    hf, hdz = ref.transfer(-1000.0, n, 0.6328, d), ref.transfer(-200.0, n, 0.6328, d)
+    ctx = _lib.default_context(0)
+    ctx.set_option(_lib.PH_OPT_FORM, _lib.PH_FORM_TUNED)
+    try:
+        p, a = ph.cu_get_reconst_xyprojection(ph.cu_gabor_wavefront(to_dev(holo, cuda)),
+                                              ph.CuTransfer(to_dev(hf, cuda)), ph.CuTransfer(to_dev(hdz, cuda)),
+                                              slices, return_argmin=True)
+    finally:
+        ctx.set_option(_lib.PH_OPT_FORM, 0)
+    p_ref, a_ref = ref.reconst_xyprojection(ref.gabor_wavefront(holo), hf, hdz, slices, with_argmin=True)
+    assert rel_l2(to_np(p), p_ref) < REL_L2 and np.mean(to_np(a) == a_ref) >= ARGMIN_AGREE
+
+
+def test_autotune_with_forms_at_2048(ph, cuda, tmp_path):
+    """With the split-precision forms allowed, the tuner times them too and
+    records whichever is fastest (the choice is a measurement, not a rule)."""
+    r = ph.autotune(2048, 2048, 64, allow_forms=True, cache=str(tmp_path / "t.json"))
+    assert r["form"] in (0, 1, 2) and r["ms"] > 0
