@@ -346,6 +346,7 @@ def main():
     ap.add_argument("--no-profile", action="store_true")
     ap.add_argument("--no-standin", action="store_true", help="skip the cuFFT stand-in of the reference sequence")
     ap.add_argument("--no-forms", action="store_true", help="skip the tensor-core forms of the row pass")
+    ap.add_argument("--no-extras", action="store_true", help="skip the brief batch (C4) and serving (C5) runs")
     ap.add_argument("--form", default="fp32", choices=["fp32", "bf16x3", "fp16x3", "fp16x2"],
                     help="arithmetic of the projection's row pass in the timed frames")
     args = ap.parse_args()
@@ -600,6 +601,13 @@ def main():
                          "on tcgen05 (FP32 accumulation, hi + lo operands); pass A, GS and labeling stay FP32. "
                          "accuracy: the CPU sample (2 GS iterations, 16 slices) against the FP32 and FP64 oracles")
 
+    # ---- the batch (C4) and serving (C5) workloads, briefly, beside the frame
+    c4 = c5 = None
+    if not args.no_extras and world == 1 and args.config == "c2":
+        ctx.set_option(_lib.PH_OPT_FORM, 0)
+        c4 = quick_c4(ph, ctx, local, cfg)
+        c5 = quick_c5(ph, ctx, local)
+
     line = {
         "metric": "reconstructed Mvoxel/s + p99 frame latency, chosen vs plain FP32 form, 1 GB300",
         "value": round(value, 2), "unit": "Mvoxel/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -621,12 +629,136 @@ def main():
         "e2e": e2e,
         "cufft_standin": standin,
         "forms": forms,
+        "c4": c4,
+        "c5": c5,
         "clocks": clk,
     }
     print(json.dumps(line))
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def quick_c4(ph, ctx, local: int, cfg: dict, steps: int = 3) -> dict:
+    """The mixed batch (96 holograms of four shapes, own slices and dz each) as a
+    planned batch against the plain per-hologram path looped on the host."""
+    import torch
+    from ph_gb300 import synth
+    c4 = CONFIGS["c4"]
+    holos, sqr = {}, {}
+    for ci, (nx, ny, _) in enumerate(C4_CLASSES):
+        spec = synth.HologramSpec(seed=c4["seed"] + 100 * ci, n=nx, n_slow=ny, count=c4["discs"], dmin=c4["dmin"],
+                                  dmax=c4["dmax"], zmin=c4["zmin"], zmax=c4["zmax"], wavlen=LAM, dx=DX)
+        holos[(nx, ny)] = synth.synth_hologram(spec, local)
+        sqr[(nx, ny)] = ph.cu_transfer_sqrt_arr(nx, LAM, DX, device=local, n_slow=ny)
+    spec_items = c4_items()
+    items = []
+    for nx, ny, S, dz in spec_items:
+        items.append({"hologram": holos[(nx, ny)], "transfer_front": ph.cu_transfer(-c4["z0"], nx, LAM, sqr[(nx, ny)]),
+                      "transfer_dz": ph.cu_transfer(-dz, nx, LAM, sqr[(nx, ny)]), "slices": S})
+    voxels = sum(nx * ny * S for nx, ny, S, _ in spec_items)
+    batch = ph.ReconBatch(items, lanes=4)
+    batch.run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        batch.run()
+    e1.record()
+    torch.cuda.synchronize()
+    bms = e0.elapsed_time(e1) / steps
+    wfs = {k: ph.cu_gabor_wavefront(h) for k, h in holos.items()}
+
+    def looped():
+        for it, (nx, ny, S, _) in zip(items, spec_items):
+            ph.cu_get_reconst_xyprojection(wfs[(nx, ny)], it["transfer_front"], it["transfer_dz"], S,
+                                           return_argmin=True)
+    looped()
+    torch.cuda.synchronize()
+    e0.record()
+    looped()
+    e1.record()
+    torch.cuda.synchronize()
+    lms = e0.elapsed_time(e1)
+    batch.close()
+    return {"workload": c4["workload"], "items": len(items), "voxels": voxels, "batch_ms": round(bms, 3),
+            "mvoxel_s": round(voxels / (bms / 1e3) / 1e6, 2), "looped_plain_ms": round(lms, 3),
+            "looped_plain_mvoxel_s": round(voxels / (lms / 1e3) / 1e6, 2), "speedup_vs_looped": round(lms / bms, 3),
+            "what": "ph_batch_plan graph over 4 lanes vs a host loop of single ph_reconst_xyproj calls (each "
+                    "with its own wavefront); device-resident, CUDA events, L2 not flushed between items"}
+
+
+def quick_c5(ph, ctx, local: int, loads=(0.5, 0.9, 1.1), nreq: int = 30) -> dict:
+    """Serving under an HBM budget: capacity from a saturated queue, then
+    Poisson arrivals at fractions of it; latency = submission to completion."""
+    import torch
+    from ph_gb300 import synth
+    c5 = CONFIGS["c5"]
+    dev = torch.device(f"cuda:{local}")
+    holos, ring = {}, {}
+    for n, S, *_ in C5_MIX:
+        spec = synth.HologramSpec(seed=c5["seed"] + n, n=n, count=c5["discs"], dmin=c5["dmin"], dmax=c5["dmax"],
+                                  zmin=c5["zmin"], zmax=c5["zmax"], wavlen=LAM, dx=DX)
+        holos[n] = synth.synth_hologram(spec, local)
+        ring[n] = [(torch.empty((n, n), dtype=torch.float32, device=dev),
+                    torch.empty((n, n), dtype=torch.int32, device=dev)) for _ in range(8)]
+    budget = 60 << 30
+    srv = ph.Server(max_shape=(2048, 2048), max_slices=512, lanes=8, budget_bytes=budget)
+    pick = [0]
+
+    def submit(kind):
+        n, S, z0, dz, _ = C5_MIX[kind]
+        p, a = ring[n][pick[0] % 8]
+        pick[0] += 1
+        return srv.submit(holos[n], p, S, z0, dz, LAM, DX, argmin=a), n * n * S
+
+    def mix(i):
+        return 0 if np.random.default_rng(5000 + i).random() < C5_MIX[0][4] else 1
+
+    for i in range(4):
+        srv.poll(submit(i % 2)[0], wait=True)
+    alone = {}
+    for kind in (0, 1):
+        lat = [srv.poll(submit(kind)[0], wait=True) for _ in range(5)]
+        alone[f"{C5_MIX[kind][0]}x{C5_MIX[kind][1]}"] = round(float(np.median(lat)), 3)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    clocks.mark_start()
+    t0 = time.perf_counter()
+    tk, vox = [], 0
+    for i in range(3 * nreq):
+        t, v = submit(mix(i))
+        tk.append(t)
+        vox += v
+    for t in tk:
+        srv.poll(t, wait=True)
+    sat = time.perf_counter() - t0
+    capacity = 3 * nreq / sat
+    rows = []
+    for load in loads:
+        rng = np.random.default_rng(6000 + int(load * 100))
+        arrivals = np.cumsum(rng.exponential(1.0 / (load * capacity), nreq))
+        start = time.perf_counter()
+        tickets = []
+        for i, at in enumerate(arrivals):
+            while time.perf_counter() - start < at:
+                pass
+            tickets.append(submit(mix(10000 + i))[0])
+        lat = [srv.poll(t, wait=True) for t in tickets]
+        rows.append({"load": load, "offered_req_s": round(load * capacity, 2),
+                     "p50_ms": round(float(np.percentile(lat, 50)), 3), "p99_ms": round(float(np.percentile(lat, 99)), 3),
+                     "requests": nreq})
+    clocks.mark_end()
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    return {"workload": c5["workload"], "capacity_req_s": round(capacity, 2),
+            "capacity_mvoxel_s": round(vox / sat / 1e6, 2), "loads": rows, "alone_p50_ms": alone,
+            "budget_bytes": budget, "peak_scratch_bytes": st["bytes_peak"], "requests_queued_at_submit": st["waited"],
+            "slots": 8, "clocks": clk,
+            "what": "ph_serve_* with admission against a 60 GiB scratch budget, 8 slots; 60 % 1024^2 x 256 / 40 % "
+                    "2048^2 x 512 requests, recurring optics (cached transfer functions)"}
 
 
 def _form_accuracy(acc: dict) -> dict:

@@ -460,15 +460,18 @@ PH_API int32_t ph_ccl_roots(ph_ctx *ctx, int64_t *roots_host, int64_t capacity, 
 /* ---- without device allocation ---------------------------------------------------- */
 
 /* No counterpart in the reference.  The component count of count_labels /
- * ph_ccl_roots for callers that cannot allocate device memory (a CUDA graph
- * being recorded, a real-time loop that forbids allocation after start-up, a
- * host that only lends registered buffers): no context, no cudaMalloc.  Its
+ * ph_ccl_roots for callers that cannot allocate device memory (a real-time
+ * acquisition loop that forbids allocation once the camera runs, a host that
+ * only lends the library buffers it registered up front): no context, no
+ * cudaMalloc.  Its
  * scratch is a fixed 256 KiB device array inside the library, present on every
  * GPU that loads it until the process exits.  count: device int64 output;
  * labels: n UInt32 labels (at most 2^28, larger n returns PH_ERR_TOO_LARGE).
  * Asynchronous on `stream` on the current device.  The first call on a device
  * looks the array's device address up and should come before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race. */
+ * capture; the address is kept for the process, so calls must not cross a
+ * cudaDeviceReset.  All calls share the array: calls that overlap on the GPU
+ * race. */
 PH_API int32_t ph_ccl_count_noalloc(int64_t *count, const uint32_t *labels, int64_t n, void *stream);
 /* Message of the last failed ph_ccl_count_noalloc call of this thread. */
 PH_API const char *ph_noalloc_last_error(void);

@@ -1,9 +1,8 @@
 // ph_noalloc.cu -- a component count that allocates no device memory.
 //
-// Some callers of this library cannot call cudaMalloc: code that records a
-// CUDA graph and may not allocate inside it, real-time acquisition loops that
-// forbid allocation once the camera is running, and hosts that only lend the
-// library buffers they registered up front.  For them, ph_ccl_count_noalloc
+// Some callers of this library cannot call cudaMalloc: real-time acquisition
+// loops that forbid allocation once the camera is running, and hosts that only
+// lend the library buffers they registered up front.  For them, ph_ccl_count_noalloc
 // gives the same count as count_labels / ph_ccl_roots without a context and
 // without any allocation: its scratch -- the per-block root counts of the scan
 // -- is a fixed device array compiled into this library.
@@ -13,7 +12,8 @@
 // the array's name as a device address (on the host it names a stand-in), so
 // the first call on each device looks its address up with
 // cudaGetSymbolAddress, with that device current, and caches it.  That first
-// call should therefore come before any stream capture.  All calls share the
+// call should therefore come before any stream capture, and calls must not
+// cross a cudaDeviceReset (which would leave the cached address stale).  All calls share the
 // one array: two calls whose work overlaps on the GPU (different streams, no
 // ordering between them) race on it and may return wrong counts.
 #include "phgb300.h"

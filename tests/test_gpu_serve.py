@@ -116,7 +116,8 @@ def test_frame_ingest_equals_host_preprocessing(ph, cuda, channels, flip):
     rows, cols, n, slices = 200, 180, 256, 12
     rng = np.random.default_rng(11)
     img = rng.integers(40, 220, (rows, cols), dtype=np.uint8)          # row-major camera frame
-    bkg = rng.uniform(0.3, 0.6, (cols, rows))                          # Float64, library layout
+    # Float64, library layout; small enough that img - bkg + offset stays positive (sqrt of it is the field)
+    bkg = rng.uniform(0.1, 0.3, (cols, rows))
     off = 64 / 255
     # host-side steps, in the library layout (image row = fast index)
     holo_small = ((img.T.astype(np.float32) / np.float32(255.0)).astype(np.float64) - bkg + off).astype(np.float32)

@@ -1,8 +1,8 @@
 """The allocation-free component count (ph_ccl_count_noalloc).
 
-Callers that may not allocate device memory -- a CUDA graph being recorded, a
-real-time acquisition loop past start-up, a host that only lends registered
-buffers -- count labeling components with ph_ccl_count_noalloc: no context, no
+Callers that may not allocate device memory -- a real-time acquisition loop
+past start-up, a host that only lends the buffers it registered up front --
+count labeling components with ph_ccl_count_noalloc: no context, no
 cudaMalloc, scratch in a fixed device array of the library.  Its count must
 equal the regular entry point's (ph_ccl_roots, i.e. count_labels) exactly, on
 two calls in a row (the second one sees the first one's leftovers in the
@@ -62,3 +62,17 @@ def test_noalloc_rejects_oversize(ph, cuda):
     st = fn(out.data_ptr(), lab.data_ptr(), (1 << 28) + 1, torch.cuda.current_stream().cuda_stream)
     assert st == _lib.PH_ERR_TOO_LARGE
     assert b"exceed" in lib.ph_noalloc_last_error()
+
+
+def test_noalloc_empty_input_counts_zero(ph, cuda):
+    """n = 0 writes a count of 0 (and launches nothing that reads labels)."""
+    from ph_gb300 import _lib
+    lib = _lib.lib()
+    fn = _noalloc(lib)
+    out = torch.full((1,), -1, dtype=torch.int64, device=cuda)
+    lab = torch.zeros((1,), dtype=torch.int32, device=cuda)
+    for _ in range(2):
+        out.fill_(-1)
+        assert fn(out.data_ptr(), lab.data_ptr(), 0, torch.cuda.current_stream().cuda_stream) == 0
+        torch.cuda.synchronize()
+        assert int(out.item()) == 0
