@@ -1625,7 +1625,7 @@ std::string dump_tune(const JsonTune &j) {
             bool first_k = true;
             for (auto &kv : sh.second) {
                 char num[64];
-                snprintf(num, sizeof num, "%.6g", kv.second);
+                snprintf(num, sizeof num, "%.9g", kv.second);
                 o += (first_k ? "" : ", ");
                 first_k = false;
                 o += "\"" + kv.first + "\": " + num;

@@ -21,14 +21,11 @@
 // per word and a tile is scaled by a power of two so that its largest value
 // is at most 2^9 (GEMM 1 grows it by at most N2 sqrt 2 < 2^15.5, inside FP16).
 //
-// A CTA (256 threads, one per SM: 224 KB of shared memory at N = 2048) owns
+// A CTA (384 threads, one per SM: 225 KB of shared memory at N = 2048) owns
 // ROWS = 128 / N2 consecutive rows y and walks the slices of its group; one
 // tile is those rows of one slice.  GEMM 1 takes 128 / N1 rows per MMA chain
-// (HALVES chains per tile), GEMM 3 the whole tile.  The MMAs of one tile run
-// while the CUDA cores split the next tile's rows (GEMM 3) or reduce the
-// previous tile (GEMM 1):
-//   per slice b:  [twiddle + split D1(b) -> A3]  GEMM3(b)  [load + split x(b+1) -> A1]
-//                 GEMM1(b+1)  [|D3(b)|^2 -> min]
+// (HALVES chains per tile), GEMM 3 the whole tile.  Warp roles and the
+// pipeline between them are described at k_recon_b_tc.
 //
 // Tables (built on the host in FP64, copied in one bulk copy per CTA): B1 and
 // B3 as swizzled K-major tiles (hi, then lo when TERMS = 3), then the twiddles
@@ -71,9 +68,11 @@ struct TcPlan {
     static constexpr uint32_t OFF_A1 = (TABLE_BYTES + 1023) / 1024 * 1024;
     static constexpr uint32_t OFF_A3 = OFF_A1 + 2 * HALVES * A1_BYTES;  // hi, lo per chain
     static constexpr uint32_t OFF_BAR = OFF_A3 + 2 * A3_BYTES;
-    static constexpr uint32_t SMEM = OFF_BAR + 128 + 1024;             // + alignment slack
-    static constexpr uint32_t TMEM_COLS = 256;                          // D1 (HALVES x NN1) + D3 (NN3)
-    static_assert(HALVES * NN1 + NN3 <= (int)TMEM_COLS, "tensor memory");
+    static constexpr uint32_t SMEM = OFF_BAR + 256 + 1024;             // + alignment slack
+    // two buffers each of D1 (HALVES x NN1 columns) and D3 (NN3 columns)
+    static constexpr uint32_t D1_COLS = HALVES * NN1, D3_COLS = NN3;
+    static constexpr uint32_t TMEM_COLS = 2 * (D1_COLS + D3_COLS) <= 256 ? 256 : 512;
+    static_assert(2 * (D1_COLS + D3_COLS) <= TMEM_COLS, "tensor memory");
     static_assert(N1 % 32 == 0 && N2 % 32 == 0 && N1 <= 64 && N2 <= 64, "N1, N2 in {32, 64}");
     static_assert(SMEM <= 227 * 1024, "shared memory");
     // epilogue: each of the two warps on a lane quarter takes half of D3's columns
@@ -99,18 +98,24 @@ __device__ __forceinline__ void split2(float x0, float x1, uint32_t &hi, uint32_
 }
 
 // Warp roles (384 threads): warps 0-7 are the consumers (8 warps, two per
-// tensor-memory lane quarter), warps 8-11 the producers.
+// tensor-memory lane quarter), warps 8-11 the producers.  D1 and D3 each have
+// two tensor-memory buffers (tile b uses buffer b & 1).
 //   producers, tile b:  wait GEMM 1 (b-1) done (A1 free) -> load + split the
 //                       rows of slice b into A1 -> barrier -> one thread waits
-//                       until the consumers have read D1 (b-1), issues GEMM 1 (b)
-//   consumers, tile b:  wait GEMM 1 (b) done -> twiddle + split D1 -> A3 ->
-//                       release D1 -> barrier -> one thread issues GEMM 3 (b) ->
-//                       wait GEMM 3 (b) done -> |D3|^2 -> running minimum
-// so the global loads of tile b + 1 run while the consumers work on tile b.
-// Hand-offs are mbarriers: GEMM 1 and GEMM 3 completion (tcgen05.commit), D1
-// released (256 consumer arrivals) and, for the FP16 forms, the row scales of
-// a tile (128 producer arrivals, two barriers alternating by tile parity so
-// that no waiter falls two phases behind).  Every wait is bounded.
+//                       until the consumers have read D1 buffer (b & 1) of
+//                       tile b-2, issues GEMM 1 (b) into it
+//   consumers, tile b:  wait GEMM 1 (b) done, and GEMM 3 (b-1) done (A3 free)
+//                       -> twiddle + split D1 -> A3 -> release that D1 buffer
+//                       -> barrier -> one thread issues GEMM 3 (b) -> reduce
+//                       tile b-1 (|D3|^2 -> running minimum) while it runs
+// so the global loads of tile b + 1 and the reduction of tile b - 1 overlap
+// the tensor pipe.  Hand-offs are mbarriers: GEMM 1 completion (one barrier
+// per D1 buffer: GEMM 1 (b + 1) may finish before the consumers wait for
+// GEMM 1 (b)), GEMM 3 completion (tcgen05.commit), each D1 buffer released
+// (256 consumer arrivals; one barrier per buffer) and, for the FP16 forms, the row scales of a tile (128
+// producer arrivals; a ring of four barriers and scale slots, as the producers
+// run at most two tiles ahead).  No waiter falls two phases behind a barrier.
+// Every wait is bounded.
 constexpr int kTcConsumers = 256, kTcProducers = 128;
 
 template <class PL>
@@ -119,11 +124,13 @@ __global__ void __launch_bounds__(384, 1) k_recon_b_tc(const ReconBTc p) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem =
         reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    // barriers: [0] tables, [1] GEMM 1 done, [2] GEMM 3 done, [3] D1 released, [4], [5] row scales
+    // barriers: [0] tables, [1], [2] GEMM 1 done per D1 buffer, [3] GEMM 3 done, [4], [5] D1 buffer
+    // released, [6..9] row scales
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + PL::OFF_BAR);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 6);
-    float *rmax = reinterpret_cast<float *>(bars + 7);          // [4 producer warps] per-warp row maxima
-    float *rscale = rmax + 4;                                    // [2][ROWS] per-row scales (FP16 forms)
+    constexpr int G1 = 1, G3 = 3, D1R = 4, SC = 6;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 10);
+    float *rmax = reinterpret_cast<float *>(bars + 11);         // [4 producer warps] per-warp row maxima
+    float *rscale = rmax + 4;                                    // [4][ROWS] per-row scales (FP16 forms)
     const float2 *tw = reinterpret_cast<const float2 *>(smem + PL::OFF_TW);
 
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -136,19 +143,20 @@ __global__ void __launch_bounds__(384, 1) k_recon_b_tc(const ReconBTc p) {
     if (warp == 0) tc::tmem_alloc(tslot, PL::TMEM_COLS);
     if (t == 0) {
         mbar_init(bars + 0, 1);
-        mbar_init(bars + 1, 1);
-        mbar_init(bars + 2, 1);
-        mbar_init(bars + 3, kTcConsumers);
-        mbar_init(bars + 4, kTcProducers);
-        mbar_init(bars + 5, kTcProducers);
+        mbar_init(bars + G1, 1);
+        mbar_init(bars + G1 + 1, 1);
+        mbar_init(bars + G3, 1);
+        mbar_init(bars + D1R, kTcConsumers);
+        mbar_init(bars + D1R + 1, kTcConsumers);
+        for (int q = 0; q < 4; ++q) mbar_init(bars + SC + q, kTcProducers);
         mbar_fence_init();
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t d1 = tmem;                              // HALVES x NN1 columns
-    const uint32_t d3 = tmem + PL::HALVES * PL::NN1;       // NN3 columns
+    auto d1 = [&](int b) { return tmem + (uint32_t)(b & 1) * PL::D1_COLS; };                       // tile b's D1
+    auto d3 = [&](int b) { return tmem + 2 * PL::D1_COLS + (uint32_t)(b & 1) * PL::D3_COLS; };   // tile b's D3
     if (t == 0) {
         mbar_arrive_expect_tx(bars + 0, PL::TABLE_BYTES);
         for (uint32_t o = 0; o < PL::TABLE_BYTES; o += 65536u) {
@@ -165,11 +173,12 @@ __global__ void __launch_bounds__(384, 1) k_recon_b_tc(const ReconBTc p) {
         const int m1 = pt;                                 // A1 row of every chain
         const int r1 = m1 / N1, n1 = m1 % N1;
         const uint32_t tile_bytes = (uint32_t)(min(PL::ROWS, p.rows - yb) * N * 8);
-        uint32_t ph1 = 0, phd = 0;
+        uint32_t ph1 = 0, phd = 0;                         // parity bits per buffer
         for (int b = b0; b < b1; ++b) {
             if (b > b0) {                                  // GEMM 1 (b - 1) has read A1
-                mbar_wait(bars + 1, ph1, p.err);
-                ph1 ^= 1u;
+                const int q = (b - 1) & 1;
+                mbar_wait(bars + G1 + q, (ph1 >> q) & 1u, p.err);
+                ph1 ^= 1u << q;
             }
             if (pt == 0 && b + 2 < b1) tc::prefetch_l2(p.t + ((size_t)(b + 2) * p.rows + yb) * N, tile_bytes);
 #pragma unroll 1
@@ -197,7 +206,7 @@ __global__ void __launch_bounds__(384, 1) k_recon_b_tc(const ReconBTc p) {
                     int e = 0;
                     frexpf(mx, &e);
                     const float sc = mx > 0.0f ? ldexpf(1.0f, 9 - e) : 1.0f;
-                    if (n1 == 0) rscale[(b & 1) * PL::ROWS + row1] = sc;
+                    if (n1 == 0) rscale[(b & 3) * PL::ROWS + row1] = sc;
 #pragma unroll
                     for (int i = 0; i < N2; ++i) v[i] = make_float2(v[i].x * sc, v[i].y * sc);
                 }
@@ -215,15 +224,16 @@ __global__ void __launch_bounds__(384, 1) k_recon_b_tc(const ReconBTc p) {
                     *reinterpret_cast<uint4 *>(alo + off) = lv;
                 }
             }
-            if constexpr (PL::FP16) mbar_arrive(bars + 4 + (b & 1));   // this tile's row scales are written
+            if constexpr (PL::FP16) mbar_arrive(bars + SC + (b & 3));  // this tile's row scales are written
             fence_proxy_async_smem();
             // every producer has written A1; stop together if any wait anywhere gave up
             const bool stop = bar_sync_or(1, kTcProducers, *errv != 0);
             if (stop) break;
             if (pt == 0) {
-                if (b > b0) {                              // the consumers have read D1 (b - 1)
-                    mbar_wait(bars + 3, phd, p.err);
-                    phd ^= 1u;
+                if (b >= b0 + 2) {                         // the consumers have read this D1 buffer (tile b - 2)
+                    const int q = b & 1;
+                    mbar_wait(bars + D1R + q, (phd >> q) & 1u, p.err);
+                    phd ^= 1u << q;
                 }
                 tc::fence_after_sync();
                 constexpr uint32_t idesc = tc::idesc_f16(128, PL::NN1, !PL::FP16);
@@ -233,7 +243,7 @@ __global__ void __launch_bounds__(384, 1) k_recon_b_tc(const ReconBTc p) {
                     const uint32_t alo = ahi + PL::A1_BYTES;
                     const uint32_t bhi = smem_addr(smem + PL::OFF_B1);
                     const uint32_t blo = bhi + PL::B1_BYTES;
-                    const uint32_t d = d1 + (uint32_t)(h * PL::NN1);
+                    const uint32_t d = d1(b) + (uint32_t)(h * PL::NN1);
 #pragma unroll
                     for (int s = 0; s < PL::K1 / 16; ++s) {
                         const uint32_t oa = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
@@ -244,7 +254,7 @@ __global__ void __launch_bounds__(384, 1) k_recon_b_tc(const ReconBTc p) {
                             tc::mma_f16(d, tc::desc_sw128(ahi + oa), tc::desc_sw128(blo + ob), idesc, true);
                     }
                 }
-                tc::mma_commit(bars + 1);
+                tc::mma_commit(bars + G1 + (b & 1));
             }
         }
     } else {
@@ -267,23 +277,45 @@ __global__ void __launch_bounds__(384, 1) k_recon_b_tc(const ReconBTc p) {
         int mink[PL::PIX];
 #pragma unroll
         for (int i = 0; i < PL::PIX; ++i) { minv[i] = __int_as_float(0x7f800000); mink[i] = 0; }
-        uint32_t ph1 = 0, ph3 = 0, phs0 = 0, phs1 = 0;
+        // |D3|^2 of tile b (in its buffer) into the running minimum
+        auto reduce = [&](int b, float inv_s2) {
+            const int k = p.k0 + b;
+            const uint32_t taddr = d3(b) + (uint32_t)(2 * k1a) + ((uint32_t)(quarter * 32) << 16);
+#pragma unroll
+            for (int c = 0; c < PL::PIX; c += 16) {
+                float v[32];
+                tc::tmem_ld32(taddr + (uint32_t)(2 * c), v);
+                tc::tmem_wait_ld();
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    float i2 = fmaf(v[2 * i], v[2 * i], v[2 * i + 1] * v[2 * i + 1]);
+                    if constexpr (PL::FP16) i2 *= inv_s2;
+                    if (i2 < minv[c + i]) { minv[c + i] = i2; mink[c + i] = k; }
+                }
+            }
+        };
+        uint32_t ph1 = 0, ph3 = 0, phs = 0;               // parity bits per barrier of a ring
+        float inv_prev = 1.0f;                             // 1 / scale^2 of tile b - 1 (FP16 forms)
+        bool stopped = false;
         for (int b = b0; b < b1; ++b) {
-            mbar_wait(bars + 1, ph1, p.err);               // GEMM 1 (b) done: D1 ready
-            ph1 ^= 1u;
+            mbar_wait(bars + G1 + (b & 1), (ph1 >> (b & 1)) & 1u, p.err);   // GEMM 1 (b) done: D1 (b) ready
+            ph1 ^= 1u << (b & 1);
             float inv_s2 = 1.0f;
             if constexpr (PL::FP16) {
-                uint32_t &ps = (b & 1) ? phs1 : phs0;
-                mbar_wait(bars + 4 + (b & 1), ps, p.err);
-                ps ^= 1u;
-                const float sc = rscale[(b & 1) * PL::ROWS + row3];
+                mbar_wait(bars + SC + (b & 3), (phs >> (b & 3)) & 1u, p.err);
+                phs ^= 1u << (b & 3);
+                const float sc = rscale[(b & 3) * PL::ROWS + row3];
                 inv_s2 = 1.0f / (sc * sc);
+            }
+            if (b > b0) {                                  // GEMM 3 (b - 1) done: A3 free, D3 (b - 1) ready
+                mbar_wait(bars + G3, ph3, p.err);
+                ph3 ^= 1u;
             }
             tc::fence_after_sync();
             {
                 unsigned char *ahi = smem + PL::OFF_A3;
                 unsigned char *alo = ahi + PL::A3_BYTES;
-                const uint32_t taddr = d1 + (uint32_t)(h1 * PL::NN1) + ((uint32_t)(quarter * 32) << 16);
+                const uint32_t taddr = d1(b) + (uint32_t)(h1 * PL::NN1) + ((uint32_t)(quarter * 32) << 16);
 #pragma unroll
                 for (int c = 0; c < K2W; c += 16) {        // 16 k2 = 32 columns per load
                     float v[32];
@@ -303,45 +335,40 @@ __global__ void __launch_bounds__(384, 1) k_recon_b_tc(const ReconBTc p) {
                 }
             }
             tc::fence_before_sync();
-            mbar_arrive(bars + 3);                         // D1 (b) read: GEMM 1 (b + 1) may write it
+            mbar_arrive(bars + D1R + (b & 1));             // D1 buffer (b & 1) read: GEMM 1 (b + 2) may write it
             fence_proxy_async_smem();
             const bool stop = bar_sync_or(2, kTcConsumers, *errv != 0);   // a uniform decision
             tc::fence_after_sync();
-            if (stop) break;
+            if (stop) {
+                stopped = true;
+                break;
+            }
             if (t == 0) {
                 constexpr uint32_t idesc = tc::idesc_f16(128, PL::NN3, !PL::FP16);
                 const uint32_t ahi = smem_addr(smem + PL::OFF_A3);
                 const uint32_t alo = ahi + PL::A3_BYTES;
                 const uint32_t bhi = smem_addr(smem + PL::OFF_B3);
                 const uint32_t blo = bhi + PL::B3_BYTES;
+                const uint32_t d = d3(b);
 #pragma unroll
                 for (int s = 0; s < PL::K3 / 16; ++s) {
                     const uint32_t oa = (uint32_t)((s >> 2) * 128 * 128 + (s & 3) * 32);
                     const uint32_t ob = (uint32_t)((s >> 2) * PL::NN3 * 128 + (s & 3) * 32);
-                    tc::mma_f16(d3, tc::desc_sw128(ahi + oa), tc::desc_sw128(bhi + ob), idesc, s > 0);
-                    tc::mma_f16(d3, tc::desc_sw128(alo + oa), tc::desc_sw128(bhi + ob), idesc, true);
+                    tc::mma_f16(d, tc::desc_sw128(ahi + oa), tc::desc_sw128(bhi + ob), idesc, s > 0);
+                    tc::mma_f16(d, tc::desc_sw128(alo + oa), tc::desc_sw128(bhi + ob), idesc, true);
                     if constexpr (PL::TERMS == 3)
-                        tc::mma_f16(d3, tc::desc_sw128(ahi + oa), tc::desc_sw128(blo + ob), idesc, true);
+                        tc::mma_f16(d, tc::desc_sw128(ahi + oa), tc::desc_sw128(blo + ob), idesc, true);
                 }
-                tc::mma_commit(bars + 2);
+                tc::mma_commit(bars + G3);
             }
-            mbar_wait(bars + 2, ph3, p.err);               // GEMM 3 (b) done: D3 ready, A3 free
-            ph3 ^= 1u;
+            if (b > b0) reduce(b - 1, inv_prev);           // while GEMM 3 (b) runs
+            inv_prev = inv_s2;
+            tc::fence_before_sync();
+        }
+        if (!stopped) {
+            mbar_wait(bars + G3, ph3, p.err);              // GEMM 3 of the last tile
             tc::fence_after_sync();
-            const int k = p.k0 + b;
-            const uint32_t taddr = d3 + (uint32_t)(2 * k1a) + ((uint32_t)(quarter * 32) << 16);
-#pragma unroll
-            for (int c = 0; c < PL::PIX; c += 16) {
-                float v[32];
-                tc::tmem_ld32(taddr + (uint32_t)(2 * c), v);
-                tc::tmem_wait_ld();
-#pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    float i2 = fmaf(v[2 * i], v[2 * i], v[2 * i + 1] * v[2 * i + 1]);
-                    if constexpr (PL::FP16) i2 *= inv_s2;
-                    if (i2 < minv[c + i]) { minv[c + i] = i2; mink[c + i] = k; }
-                }
-            }
+            reduce(b1 - 1, inv_prev);
             tc::fence_before_sync();
         }
         if (valid3) {
