@@ -1077,18 +1077,117 @@ int serve_transfer(ph_server *srv, cudaStream_t ls, float *dsqr, int nx, int ny,
 }
 
 // Longest-processing-time assignment of items (work = pixels x slices) to lanes.
-std::vector<int> assign_lanes(const ph_recon_item *items, int count, int lanes) {
-    std::vector<int> order(count), lane(count, 0);
-    for (int i = 0; i < count; ++i) order[i] = i;
-    auto work = [&](int i) { return (double)items[i].n_fast * items[i].n_slow * items[i].slices; };
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return work(a) > work(b); });
-    std::vector<double> load(lanes, 0.0);
-    for (int i : order) {
-        const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        lane[i] = l;
-        load[l] += work(i);
+// A group of batch items of one transform shape and input kind, issued as one
+// launch of each pass (grid z = item): the forward rows, the spectrum, and per
+// slice batch pass A and pass B, then each item's projection.  Items sit in
+// consecutive scratch slots of `item_bytes` from `base`.  Every item gets the
+// slice batches and slice groups of a single ph_reconst_xyproj call over its
+// own slices, so its results equal that call's exactly.
+size_t group_item_bytes(ph_ctx *ctx, int nx, int ny, int max_slices) {
+    const ReconLayout L = recon_layout(ctx, nx, ny, ny, nx, max_slices, kLaneBatchBytes);
+    return (L.total + kAlign - 1) / kAlign * kAlign;
+}
+
+int issue_recon_group(ph_ctx *ctx, const std::vector<const ph_recon_item *> &its, char *base, cudaStream_t s) {
+    const int G = (int)its.size();
+    const int nx = its[0]->n_fast, ny = its[0]->n_slow;
+    int smax = 0;
+    for (auto *it : its) smax = std::max(smax, (int)it->slices);
+    const ReconLayout L = recon_layout(ctx, nx, ny, ny, nx, smax, kLaneBatchBytes);
+    const size_t ib = group_item_bytes(ctx, nx, ny, smax);
+    auto slot = [&](int i, size_t off) { return base + (size_t)i * ib + off; };
+    const float2 *tw_x = ctx->tw[nx], *tw_y = ctx->tw[ny];
+    // forward rows (the wavefront sqrt(I) formed in the first stage for hologram items)
+    if (its[0]->hologram != nullptr) {
+        FwdRowsT<FWD_SQRT_REAL> f{};
+        f.src_real = its[0]->hologram;
+        for (int i = 0; i < G; ++i) f.src_real_items[i] = its[i]->hologram;
+        f.dst = reinterpret_cast<float2 *>(slot(0, L.a1));
+        f.dst_stride = ib / sizeof(float2);
+        f.tw = tw_x;
+        f.nrows = ny;
+        f.nitems = G;
+        PH_TRY(pass(ctx, s, "fwd_rows", [&] { return launch_fwd_rows(nx, f, s); }));
+    } else {
+        FwdRowsT<FWD_COMPLEX> f{};
+        f.src = static_cast<const float2 *>(its[0]->wavefront);
+        for (int i = 0; i < G; ++i) f.src_items[i] = static_cast<const float2 *>(its[i]->wavefront);
+        f.dst = reinterpret_cast<float2 *>(slot(0, L.a1));
+        f.dst_stride = ib / sizeof(float2);
+        f.tw = tw_x;
+        f.nrows = ny;
+        f.nitems = G;
+        PH_TRY(pass(ctx, s, "fwd_rows", [&] { return launch_fwd_rows(nx, f, s); }));
     }
-    return lane;
+    SpectrumCols c{};
+    c.a1 = reinterpret_cast<const float2 *>(slot(0, L.a1));
+    c.hf = static_cast<const float2 *>(its[0]->tf_front);
+    c.hdz = static_cast<const float2 *>(its[0]->tf_dz);
+    for (int i = 0; i < G; ++i) {
+        c.hf_items[i] = static_cast<const float2 *>(its[i]->tf_front);
+        c.hdz_items[i] = static_cast<const float2 *>(its[i]->tf_dz);
+    }
+    c.lpf = nullptr;
+    c.ptab = ctx->phase_tab;
+    c.state = reinterpret_cast<float4 *>(slot(0, L.state));
+    c.a1_stride = ib / sizeof(float2);
+    c.state_stride = ib / sizeof(float4);
+    c.tw = tw_y;
+    c.nx = nx;
+    c.ny = ny;
+    c.scale = (float)(1.0 / ((double)nx * (double)ny));
+    c.nitems = G;
+    PH_TRY(pass(ctx, s, "spectrum", [&] { return launch_spectrum(ny, c, s); }));
+    const size_t npix = (size_t)nx * ny;
+    for (int i = 0; i < G; ++i)
+        PH_CUDA(cudaMemsetAsync(slot(i, L.p64), 0xff, sizeof(unsigned long long) * npix, s), "cudaMemsetAsync");
+    const int row_blocks_a = (nx + recon_a_rows(ny) - 1) / recon_a_rows(ny);
+    const ph_tuning *tu = tuning_of(ctx, nx, ny);
+    for (int k0 = 0; k0 < smax; k0 += L.batch) {
+        ReconA a{};
+        ReconB<EPI_PROJ> b{};
+        for (int i = 0; i < G; ++i) {
+            const int nb = std::max(0, std::min(L.batch, (int)its[i]->slices - k0));
+            const int grp = nb > 0 ? recon_group(nb, row_blocks_a, recon_a_chain(ny), tu ? tu->group_cap : 0) : 1;
+            a.nb_items[i] = b.nb_items[i] = nb;
+            a.group_items[i] = b.group_items[i] = grp;
+        }
+        a.state = reinterpret_cast<const float4 *>(slot(0, L.state));
+        a.t = reinterpret_cast<float2 *>(slot(0, L.t));
+        a.item_state_stride = ib / sizeof(float4);
+        a.item_t_stride = ib / sizeof(float2);
+        a.tw = tw_y;
+        a.nx = nx;
+        a.ny_out = ny;
+        a.y0 = 0;
+        a.k0 = k0;
+        a.nbatch = a.nb_items[0];   // item 0 has the most slices
+        a.group = a.group_items[0];
+        a.nitems = G;
+        a.err = static_cast<int *>(ctx->small);
+        PH_TRY(pass(ctx, s, "recon_a", [&] { return launch_recon_a(ny, a, a.nbatch, s); }));
+        b.t = reinterpret_cast<const float2 *>(slot(0, L.t));
+        b.tw = tw_x;
+        b.proj64 = reinterpret_cast<unsigned long long *>(slot(0, L.p64));
+        b.t_stride = ib / sizeof(float2);
+        b.p64_stride = ib / sizeof(unsigned long long);
+        b.rows = ny;
+        b.nx_out = nx;
+        b.x0 = 0;
+        b.k0 = k0;
+        b.nbatch = b.nb_items[0];
+        b.group = b.group_items[0];
+        b.vol_slice_stride = (long long)npix;
+        b.nitems = G;
+        b.err = static_cast<int *>(ctx->small);
+        PH_TRY(pass(ctx, s, "recon_b", [&] { return launch_recon_b(nx, b, s); }));
+    }
+    for (int i = 0; i < G; ++i) {
+        k_proj_finish<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(
+            reinterpret_cast<const unsigned long long *>(slot(i, L.p64)), its[i]->proj, its[i]->argmin, npix);
+        PH_TRY(launched(ctx, cudaGetLastError(), "projection finish"));
+    }
+    return PH_OK;
 }
 
 }  // namespace
@@ -1852,19 +1951,61 @@ int32_t ph_batch_plan(ph_ctx *ctx, const ph_recon_item *items, int32_t count, in
         if (it.slices < 1) { set_err(ctx, "item %d: slices must be >= 1. Got %d.", i, it.slices); return PH_ERR_SIZE; }
         PH_TRY(check_len(ctx, it.n_fast, it.n_slow));
     }
-    lanes = std::max(1, std::min(lanes, std::max(count, 1)));
+    // Groups: items of one transform shape and input kind, most slices first,
+    // up to kMaxItems per group and kGroupBytes of scratch, share one launch
+    // of each pass.  (A shape whose projection runs a tensor-core row pass
+    // keeps one item per group: that pass has no grouped form.)
+    constexpr size_t kGroupBytes = size_t(8) << 30;
+    std::map<std::tuple<int, int, int>, std::vector<int>> classes;
+    for (int i = 0; i < count; ++i)
+        classes[{items[i].n_fast, items[i].n_slow, items[i].hologram != nullptr ? 1 : 0}].push_back(i);
+    std::vector<std::vector<int>> groups;
+    for (auto &kv : classes) {
+        auto &v = kv.second;
+        std::stable_sort(v.begin(), v.end(), [&](int a, int c) { return items[a].slices > items[c].slices; });
+        const int nx = std::get<0>(kv.first), ny = std::get<1>(kv.first);
+        const bool tc = effective_form(ctx, nx, ny) != PH_FORM_FP32;
+        for (size_t k = 0; k < v.size();) {
+            const size_t ib = group_item_bytes(ctx, nx, ny, items[v[k]].slices);
+            const size_t gmax = tc ? 1 : std::max<size_t>(1, std::min<size_t>(kMaxItems, kGroupBytes / ib));
+            const size_t n = std::min(gmax, v.size() - k);
+            groups.emplace_back(v.begin() + k, v.begin() + k + n);
+            k += n;
+        }
+    }
+    const int ngroups = (int)groups.size();
+    lanes = std::max(1, std::min(lanes, std::max(ngroups, 1)));
     auto *b = new ph_batch();
     b->ctx = ctx;
     b->items.assign(items, items + count);
-    b->lane_of = assign_lanes(items, count, lanes);
     b->lanes = lanes;
-    // per-lane scratch: the largest layout among the lane's items
-    std::vector<size_t> lane_bytes(lanes, 0), lane_off(lanes, 0);
-    for (int i = 0; i < count; ++i) {
-        const ReconLayout L = recon_layout(ctx, items[i].n_fast, items[i].n_slow, items[i].n_slow, items[i].n_fast,
-                                           items[i].slices, kLaneBatchBytes);
-        lane_bytes[b->lane_of[i]] = std::max(lane_bytes[b->lane_of[i]], L.total);
+    // longest-processing-time assignment of the groups to lanes (work = pixels x slices)
+    std::vector<int> group_lane(ngroups, 0), gorder(ngroups);
+    {
+        auto work = [&](int g) {
+            double w = 0.0;
+            for (int i : groups[g]) w += (double)items[i].n_fast * items[i].n_slow * items[i].slices;
+            return w;
+        };
+        for (int g = 0; g < ngroups; ++g) gorder[g] = g;
+        std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int c) { return work(a) > work(c); });
+        std::vector<double> load(lanes, 0.0);
+        for (int g : gorder) {
+            const int l = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            group_lane[g] = l;
+            load[l] += work(g);
+        }
     }
+    b->lane_of.assign(count, 0);
+    for (int g = 0; g < ngroups; ++g)
+        for (int i : groups[g]) b->lane_of[i] = group_lane[g];
+    // per-lane scratch: the largest group among the lane's groups
+    auto group_bytes = [&](int g) {
+        const ph_recon_item &f = items[groups[g][0]];
+        return groups[g].size() * group_item_bytes(ctx, f.n_fast, f.n_slow, f.slices);
+    };
+    std::vector<size_t> lane_bytes(lanes, 0), lane_off(lanes, 0);
+    for (int g = 0; g < ngroups; ++g) lane_bytes[group_lane[g]] = std::max(lane_bytes[group_lane[g]], group_bytes(g));
     size_t total = 0;
     for (int l = 0; l < lanes; ++l) {
         lane_off[l] = total;
@@ -1913,9 +2054,15 @@ int32_t ph_batch_plan(ph_ctx *ctx, const ph_recon_item *items, int32_t count, in
     for (int l = 0; l < lanes && st == PH_OK; ++l) {
         cudaStreamWaitEvent(ls[l], fork, 0);
         char *base = static_cast<char *>(b->scratch) + lane_off[l];
-        for (int i = 0; i < count && st == PH_OK; ++i) {
-            if (b->lane_of[i] != l) continue;
-            const ph_recon_item &it = items[i];
+        for (int g = 0; g < ngroups && st == PH_OK; ++g) {
+            if (group_lane[g] != l) continue;
+            if (groups[g].size() > 1) {
+                std::vector<const ph_recon_item *> its;
+                for (int i : groups[g]) its.push_back(&items[i]);
+                st = issue_recon_group(ctx, its, base, ls[l]);
+                continue;
+            }
+            const ph_recon_item &it = items[groups[g][0]];
             const int nx = it.n_fast, ny = it.n_slow;
             const ReconLayout L = recon_layout(ctx, nx, ny, ny, nx, it.slices, kLaneBatchBytes);
             const float2 *tw_x = ctx->tw[nx], *tw_y = ctx->tw[ny];

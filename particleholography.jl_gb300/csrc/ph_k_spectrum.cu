@@ -4,7 +4,7 @@
 namespace ph {
 
 cudaError_t launch_spectrum(int n, const SpectrumCols &b, cudaStream_t s) {
-    return launch_len<true>(n, b, b.nx, 1, s);
+    return launch_len<true>(n, b, b.nx, 1, s, b.nitems);
 }
 
 }  // namespace ph

@@ -2,6 +2,8 @@
 // compiled for it, and the launch helpers the entry points call.
 #pragma once
 
+#include <algorithm>
+
 #include "ph_passes.cuh"
 
 namespace ph {
@@ -28,7 +30,7 @@ inline int rows_per_cta(int n) {
 }
 
 template <int N, bool ROW_FAST, class Body>
-cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) {
+cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s, int grid_z = 1) {
     static_assert(Body::EPT == PassBase::EPT, "the twiddle table is laid out for the common plan");
     auto kern = k_pass<N, ROW_FAST, Body>;
     constexpr size_t smem = Body::template smem<N, ROW_FAST>();
@@ -68,7 +70,7 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) 
     constexpr int CS = Body::template cluster<N>();
     if constexpr (CS > 1) {
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((gx + CS - 1) / CS * CS, grid_y);
+        cfg.gridDim = dim3((gx + CS - 1) / CS * CS, grid_y, grid_z);
         cfg.blockDim = dim3(S::THREADS);
         cfg.dynamicSmemBytes = smem;
         cfg.stream = s;
@@ -85,7 +87,7 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) 
         // programmatic dependent launch: the grid may start while the previous
         // kernel on the stream finishes (the body waits before touching its data)
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(gx, grid_y);
+        cfg.gridDim = dim3(gx, grid_y, grid_z);
         cfg.blockDim = dim3(S::THREADS);
         cfg.dynamicSmemBytes = smem;
         cfg.stream = s;
@@ -96,7 +98,7 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s) 
         cfg.numAttrs = 1;
         return cudaLaunchKernelEx(&cfg, kern, body);
     }
-    dim3 grid(gx, grid_y);
+    dim3 grid(gx, grid_y, grid_z);
     kern<<<grid, S::THREADS, smem, s>>>(body);
     return cudaGetLastError();
 }
@@ -126,9 +128,9 @@ bool staged_len(int n) {
 }
 
 template <bool ROW_FAST, class Body>
-cudaError_t launch_len(int n, const Body &body, int nrows, int grid_y, cudaStream_t s) {
+cudaError_t launch_len(int n, const Body &body, int nrows, int grid_y, cudaStream_t s, int grid_z = 1) {
     switch (n) {
-#define PH_LAUNCH_CASE(N) case N: return launch_one<N, ROW_FAST>(body, nrows, grid_y, s);
+#define PH_LAUNCH_CASE(N) case N: return launch_one<N, ROW_FAST>(body, nrows, grid_y, s, grid_z);
         PH_FOR_EACH_N(PH_LAUNCH_CASE)
 #undef PH_LAUNCH_CASE
     }
@@ -137,6 +139,7 @@ cudaError_t launch_len(int n, const Body &body, int nrows, int grid_y, cudaStrea
 
 // ---- launchers, one translation unit each (compiled in parallel)
 
+// (grouped launches: grid z = b.nitems; pass A / pass B grid y = the largest item's slice groups)
 cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_COMPLEX> &b, cudaStream_t s);
 cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_SQRT_REAL> &b, cudaStream_t s);
 cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_PADDED> &b, cudaStream_t s);

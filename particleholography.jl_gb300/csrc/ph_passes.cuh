@@ -146,6 +146,17 @@ __device__ __forceinline__ int shift_idx(int i, int n) {   // centred index of n
     return s >= n ? s - n : s;
 }
 
+// ---------------------------------------------------------------- grouped launches
+
+// A grouped launch runs one pass for up to kMaxItems holograms of the same
+// transform shape at once: blockIdx.z is the item.  Each item has its own
+// input and transfer functions (pointer tables in the pass's parameters), its
+// own slot of the scratch (the pass's pointers plus z times a stride) and its
+// own slice count within the batch (nb_items) and slices per CTA
+// (group_items), so every item is computed exactly as a single call would.
+// With nitems = 1 (every single call) the tables are unused.
+constexpr int kMaxItems = 8;
+
 // ---------------------------------------------------------------- forward rows (transposed store)
 
 enum FwdInput { FWD_COMPLEX = 0, FWD_SQRT_REAL = 1, FWD_PADDED = 2 };
@@ -162,10 +173,18 @@ struct FwdRowsT : PassBase {
     const float2 *pad_mean;   // device scalar (FWD_PADDED)
     int nrows;                // rows of the (virtual) input = ny
     int nx_in, ny_in, pad_off;
+    int nitems = 1;           // grouped launch: item z reads src_items / src_real_items[z], writes dst + z dst_stride
+    size_t dst_stride = 0;
+    const float2 *src_items[kMaxItems] = {};
+    const float *src_real_items[kMaxItems] = {};
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
         using S = Shape<N, EPT, TT>;
+        const int z = blockIdx.z;
+        const float2 *src = nitems > 1 ? src_items[z] : this->src;
+        const float *src_real = nitems > 1 ? src_real_items[z] : this->src_real;
+        float2 *dst = this->dst + (size_t)z * dst_stride;
         const int y = blockIdx.x * S::ROWS + r;
         const bool valid = y < nrows;
         float2 mean = make_float2(0.f, 0.f);
@@ -232,10 +251,19 @@ struct SpectrumCols : PassBase {
     const float2 *tw;
     int nx, ny;
     float scale;
+    int nitems = 1;          // grouped launch: item z's transfers from the tables, a1 / state + z strides
+    size_t a1_stride = 0, state_stride = 0;
+    const float2 *hf_items[kMaxItems] = {};
+    const float2 *hdz_items[kMaxItems] = {};
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
         using S = Shape<N, EPT, TT>;
+        const int z = blockIdx.z;
+        const float2 *a1 = this->a1 + (size_t)z * a1_stride;
+        float4 *state = this->state + (size_t)z * state_stride;
+        const float2 *hf = nitems > 1 ? hf_items[z] : this->hf;
+        const float2 *hdz = nitems > 1 ? hdz_items[z] : this->hdz;
         const int kx = blockIdx.x * S::ROWS + r;
         const bool valid = kx < nx;
         const int sx = valid ? shift_idx(kx, nx) : 0;
@@ -286,6 +314,9 @@ struct ReconA : PassBase {
     int nx, ny_out, y0;
     int k0;                // global slice index of batch slot 0
     int nbatch, group;     // slices in the batch, slices per CTA
+    int nitems = 1;        // grouped launch: item z's state / t + z strides, its slices and group
+    size_t item_state_stride = 0, item_t_stride = 0;
+    int nb_items[kMaxItems] = {}, group_items[kMaxItems] = {};
 
     // Staged forms, the first that fits the CTA's shared memory beside the
     // exchange rows:
@@ -376,8 +407,13 @@ struct ReconA : PassBase {
         const int kx0 = (CS == 1 ? lin / gridDim.y : blockIdx.x) * ROWS;
         const int kx = kx0 + r;
         const bool valid = kx < nx;   // (CTAs that only pad a cluster hold no valid row)
+        const int z = blockIdx.z;
+        const int group = nitems > 1 ? group_items[z] : this->group;
         const int b0 = g * group;
-        const int b1 = min(b0 + group, nbatch);
+        const int b1 = min(b0 + group, nitems > 1 ? nb_items[z] : nbatch);
+        if (b0 >= b1) return;   // (an item with fewer slices; uniform over a cluster, which shares z and g)
+        const float4 *state = this->state + (size_t)z * item_state_stride;
+        float2 *t = this->t + (size_t)z * item_t_stride;
         const float4 *srow = state + (size_t)(valid ? kx : 0) * N;
         float2 *xs = nullptr, *hs = nullptr;
         if constexpr (FORM == FORM_CHAIN) {
@@ -541,6 +577,9 @@ struct ReconB : PassBase {
     int nx_out, x0;                  // stored columns [x0, x0 + nx_out)
     int k0, nbatch, group;
     long long vol_slice_stride;      // elements per stored slice
+    int nitems = 1;                  // grouped launch (EPI_PROJ): item z's t / proj64 + z strides, slices, group
+    size_t t_stride = 0, p64_stride = 0;
+    int nb_items[kMaxItems] = {}, group_items[kMaxItems] = {};
 
     // One buffer: the exchange rows (which also hold the dense bulk-copied rows).
     template <int N, bool RF>
@@ -568,8 +607,13 @@ struct ReconB : PassBase {
         const int yb = blockIdx.x * ROWS;
         const int y = yb + r;
         const bool valid = y < rows;
+        const int z = blockIdx.z;
+        const int group = nitems > 1 ? group_items[z] : this->group;
         const int b0 = blockIdx.y * group;
-        const int b1 = min(b0 + group, nbatch);
+        const int b1 = min(b0 + group, nitems > 1 ? nb_items[z] : nbatch);
+        if (b0 >= b1) return;   // (an item with fewer slices)
+        const float2 *t = this->t + (size_t)z * t_stride;
+        unsigned long long *proj64 = this->proj64 == nullptr ? nullptr : this->proj64 + (size_t)z * p64_stride;
         const int nvalid = min(ROWS, rows - yb);
         auto issue = [&](int b, int buf) {   // one thread: the rows of slice b into buffer buf
             fence_proxy_async_smem();

@@ -50,6 +50,32 @@ def test_batch_equals_single_calls(ph, cuda, lanes):
     batch.close()
 
 
+def test_grouped_items_equal_single_calls(ph, cuda):
+    """Items of one shape share one launch of each pass (grid z = item, up to 8
+    per group): own inputs, transfer functions and slice counts, including the
+    2048 product-chain form and more items than one group holds.  Each equals
+    its single call bit for bit (both with 64-slice batches of intermediates,
+    so the product chains restart at the same slices)."""
+    from ph_gb300 import _lib
+    spec = [(256, 256, sl, True) for sl in (1, 5, 33, 64, 100, 7, 2, 200, 50, 3)]
+    spec += [(2048, 2048, sl, True) for sl in (96, 40, 200)]
+    spec += [(1024, 512, sl, False) for sl in (12, 70, 1)]
+    items = [_item(cuda, nx, ny, sl, seed=20 + i, as_hologram=h)[0] for i, (nx, ny, sl, h) in enumerate(spec)]
+    ctx = _lib.default_context(0)
+    ctx.set_option(_lib.PH_OPT_SLICE_BATCH, 64)
+    try:
+        batch = ph.ReconBatch(items, lanes=3)
+        proj, arg = batch.run()
+        torch.cuda.synchronize()
+        for it, p, a in zip(items, proj, arg):
+            p1, a1 = _single(ph, it)
+            assert torch.equal(p, p1), it["slices"]
+            assert torch.equal(a, a1), it["slices"]
+        batch.close()
+    finally:
+        ctx.set_option(_lib.PH_OPT_SLICE_BATCH, 0)
+
+
 def test_batch_against_oracle_and_replay(ph, cuda):
     it0, holo0, hf0, hdz0 = _item(cuda, 256, 256, 12, seed=5, as_hologram=True)
     it1, holo1, hf1, hdz1 = _item(cuda, 128, 64, 7, seed=6, as_hologram=False)
