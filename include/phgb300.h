@@ -378,11 +378,13 @@ PH_API int32_t ph_serve_submit(ph_server *srv, const ph_serve_request *req, int6
  * PH_PENDING if not yet (wait = 0), or waits for it (wait = 1), admitting
  * queued requests as earlier ones finish.  No reference counterpart. */
 PH_API int32_t ph_serve_poll(ph_server *srv, int64_t ticket, int32_t wait, double *latency_ms);
-/* Requests queued and running, pool bytes in use and at peak, and the number of
- * requests that had to queue at submission (each pointer nullable).
- * (no reference counterpart) */
+/* Requests queued and running, pool bytes in use and at peak, the number of
+ * requests that had to queue at submission, and the number admitted in shared
+ * launches: requests of the same shape, slices and optics queued together are
+ * admitted as one group (up to 8) on one slot and one block, and share one
+ * launch of each pass (each pointer nullable).  (no reference counterpart) */
 PH_API int32_t ph_serve_stats(ph_server *srv, int64_t *queued, int64_t *running, size_t *bytes_in_use,
-                              size_t *bytes_peak, int64_t *waited);
+                              size_t *bytes_peak, int64_t *waited, int64_t *grouped);
 /* Runs every queued request to completion, frees the server (no reference counterpart). */
 PH_API void ph_serve_destroy(ph_server *srv);
 

@@ -90,7 +90,8 @@ SIGNATURES = {
     "ph_batch_scratch_bytes": (_sz, [_vp]),
     "ph_batch_destroy": (None, [_vp]),
     "ph_serve_create": (_i32, [_vp, _i32, _i32, _i32, _i32, _i32, _sz, ctypes.POINTER(_vp)]),
-    "ph_serve_stats": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_sz), ctypes.POINTER(_sz), ctypes.POINTER(_i64)]),
+    "ph_serve_stats": (_i32, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_sz), ctypes.POINTER(_sz),
+                              ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "ph_serve_submit": (_i32, [_vp, _vp, ctypes.POINTER(_i64), _vp]),
     "ph_serve_poll": (_i32, [_vp, _i64, _i32, ctypes.POINTER(_f64)]),
     "ph_serve_destroy": (None, [_vp]),

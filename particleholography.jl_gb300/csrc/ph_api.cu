@@ -39,8 +39,9 @@ struct ph_serve_ticket {
     cudaEvent_t submitted = nullptr;   // on the caller's stream at submission: the inputs are written
     cudaEvent_t ev = nullptr;          // on the slot's stream after the completion callback
     int slot = -1;                     // -1 while queued
-    size_t off = 0, bytes = 0;         // the request's block of the pool
+    size_t off = 0, bytes = 0;         // the request's block of the pool (0 for a group's other members)
     bool harvested = false;            // its slot and block have been given back
+    std::vector<ph_serve_ticket *> members;   // a group's leader: the other requests sharing its launches
 };
 
 struct ph_serve_tf {
@@ -70,6 +71,7 @@ struct ph_server {
     std::unordered_map<int64_t, ph_serve_ticket *> tickets;
     std::vector<cudaEvent_t> event_pool;
     int64_t admitted_total = 0, waited_total = 0;   // requests admitted; of them, ones that had to queue
+    int64_t grouped_total = 0;                        // requests admitted in shared launches
 };
 
 // A planned batch of reconstructions: its items, lanes, own scratch and the
@@ -1013,10 +1015,16 @@ double now_s() {
 
 void CUDART_CB serve_done(void *p) {   // host callback: no CUDA calls here
     auto *t = static_cast<ph_serve_ticket *>(p);
-    t->t_done = now_s();
-    t->done.store(1, std::memory_order_release);
+    const double now = now_s();
+    t->t_done = now;
+    for (auto *m : t->members) m->t_done = now;
     std::lock_guard<std::mutex> lk(t->srv->cmu);   // held briefly, never around a CUDA call
+    t->done.store(1, std::memory_order_release);
     t->srv->completed.push_back(t);
+    for (auto *m : t->members) {
+        m->done.store(1, std::memory_order_release);
+        t->srv->completed.push_back(m);
+    }
 }
 
 cudaEvent_t serve_event(ph_server *srv) {
@@ -2188,10 +2196,60 @@ void serve_harvest(ph_server *srv) {
     }
     for (auto *t : done) {
         if (t->harvested) continue;
-        pool_free(srv, t->off, t->bytes);
-        srv->slot_job[t->slot] = nullptr;
+        if (t->bytes > 0) pool_free(srv, t->off, t->bytes);
+        if (srv->slot_job[t->slot] == t) srv->slot_job[t->slot] = nullptr;
         t->harvested = true;
     }
+}
+
+// Same-shape requests with the same optics: one group, one launch of each pass.
+bool serve_same_group(const ph_serve_request &a, const ph_serve_request &b) {
+    return a.frame == nullptr && b.frame == nullptr && a.n_fast == b.n_fast && a.n_slow == b.n_slow &&
+           a.slices == b.slices && a.z0 == b.z0 && a.dz == b.dz && a.wavlen == b.wavlen && a.dx == b.dx;
+}
+
+// Bytes of a group of g requests' block: their reconstruction slots and the
+// transfer builder's plane.
+size_t serve_group_bytes(ph_ctx *ctx, int nx, int ny, int slices, int g) {
+    const size_t plane = ((size_t)nx * ny * sizeof(float) + kAlign - 1) / kAlign * kAlign;
+    return (size_t)g * group_item_bytes(ctx, nx, ny, slices) + plane + kAlign;
+}
+
+// Issues an admitted group (leader + members) on the leader's slot.
+int serve_issue_group(ph_server *srv, ph_serve_ticket *lead) {
+    ph_ctx *ctx = srv->ctx;
+    const ph_serve_request &rq = lead->req;
+    const int nx = rq.n_fast, ny = rq.n_slow;
+    cudaStream_t ls = srv->streams[lead->slot];
+    std::vector<ph_serve_ticket *> all{lead};
+    all.insert(all.end(), lead->members.begin(), lead->members.end());
+    for (auto *m : all) PH_CUDA(cudaStreamWaitEvent(ls, m->submitted, 0), "cudaStreamWaitEvent");
+    char *base = static_cast<char *>(srv->pool) + lead->off;
+    float *dsqr = reinterpret_cast<float *>(base + all.size() * group_item_bytes(ctx, nx, ny, rq.slices));
+    for (int n : {nx, ny}) {
+        if (ctx->tw.find(n) == ctx->tw.end()) {
+            const float2 *tw = nullptr;
+            PH_TRY(get_twiddles(ctx, n, ls, &tw));
+            PH_CUDA(cudaStreamSynchronize(ls), "cudaStreamSynchronize");
+        }
+    }
+    const float2 *hf = nullptr, *hdz = nullptr;
+    ph_serve_tf *ef = nullptr, *ed = nullptr;
+    PH_TRY(serve_transfer(srv, ls, dsqr, nx, ny, rq.z0, rq.wavlen, rq.dx, &hf, &ef));
+    PH_TRY(serve_transfer(srv, ls, dsqr, nx, ny, rq.dz, rq.wavlen, rq.dx, &hdz, &ed));
+    std::vector<ph_recon_item> items(all.size());
+    std::vector<const ph_recon_item *> its;
+    for (size_t i = 0; i < all.size(); ++i) {
+        const ph_serve_request &r = all[i]->req;
+        items[i] = ph_recon_item{r.hologram, nullptr, hf, hdz, r.proj, r.argmin, nx, ny, r.slices};
+        its.push_back(&items[i]);
+    }
+    PH_TRY(issue_recon_group(ctx, its, base, ls));
+    cudaEventRecord(ef->last_use, ls);
+    cudaEventRecord(ed->last_use, ls);
+    PH_CUDA(cudaLaunchHostFunc(ls, serve_done, lead), "cudaLaunchHostFunc");
+    for (auto *m : all) PH_CUDA(cudaEventRecord(m->ev, ls), "cudaEventRecord");
+    return PH_OK;
 }
 
 // Issues one admitted request on its slot's stream.
@@ -2266,7 +2324,53 @@ int serve_dispatch(ph_server *srv) {
         for (int l = 0; l < srv->lanes; ++l)
             if (srv->slot_job[l] == nullptr) { slot = l; break; }
         if (slot < 0) return PH_OK;
+        // Requests of the same shape and optics queued right behind it share its
+        // launches (their projection runs the FP32 row pass, which has a grouped form).
+        int g = 1;
+        while (g < (int)srv->pending.size() && g < kMaxItems && serve_same_group(t->req, srv->pending[g]->req)) ++g;
+        if (g > 1 && effective_form(srv->ctx, t->req.n_fast, t->req.n_slow) != PH_FORM_FP32) g = 1;
         size_t off = 0;
+        while (g > 1) {
+            const size_t gb = serve_group_bytes(srv->ctx, t->req.n_fast, t->req.n_slow, t->req.slices, g);
+            if (gb <= srv->pool_bytes && pool_alloc(srv, gb, &off)) {
+                t->bytes = gb;
+                break;
+            }
+            --g;
+        }
+        if (g > 1) {
+            srv->pending.pop_front();
+            t->members.clear();
+            for (int i = 1; i < g; ++i) {
+                ph_serve_ticket *m = srv->pending.front();
+                srv->pending.pop_front();
+                m->slot = slot;
+                m->off = off;
+                m->bytes = 0;
+                m->t_admit = now_s();
+                t->members.push_back(m);
+            }
+            t->slot = slot;
+            t->off = off;
+            t->t_admit = now_s();
+            srv->slot_job[slot] = t;
+            srv->admitted_total += g;
+            srv->grouped_total += g;
+            const int st = serve_issue_group(srv, t);
+            if (st != PH_OK) {
+                pool_free(srv, t->off, t->bytes);
+                srv->slot_job[slot] = nullptr;
+                for (auto *m : t->members) {
+                    m->harvested = true;
+                    m->done.store(-1, std::memory_order_release);
+                }
+                t->members.clear();
+                t->harvested = true;
+                t->done.store(-1, std::memory_order_release);
+                return st;
+            }
+            continue;
+        }
         if (!pool_alloc(srv, t->bytes, &off)) return PH_OK;   // waits for memory to free up
         srv->pending.pop_front();
         t->slot = slot;
@@ -2455,7 +2559,7 @@ int32_t ph_serve_poll(ph_server *srv, int64_t ticket, int32_t wait, double *late
 }
 
 int32_t ph_serve_stats(ph_server *srv, int64_t *queued, int64_t *running, size_t *bytes_in_use, size_t *bytes_peak,
-                       int64_t *waited) {
+                       int64_t *waited, int64_t *grouped) {
     if (srv == nullptr) return PH_ERR_INVALID;
     std::lock_guard<std::mutex> lk(srv->mu);
     {
@@ -2470,6 +2574,7 @@ int32_t ph_serve_stats(ph_server *srv, int64_t *queued, int64_t *running, size_t
     if (bytes_in_use) *bytes_in_use = srv->used;
     if (bytes_peak) *bytes_peak = srv->peak;
     if (waited) *waited = srv->waited_total;
+    if (grouped) *grouped = srv->grouped_total;
     return PH_OK;
 }
 

@@ -87,14 +87,16 @@ class Server:
         return t.value
 
     def stats(self) -> dict:
-        """Requests queued and running, pool bytes in use and at peak, and how
-        many requests had to queue at submission."""
-        q, r, w = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        """Requests queued and running, pool bytes in use and at peak, how many
+        requests had to queue at submission, and how many were admitted in
+        shared launches (same shape, slices and optics, queued together)."""
+        q, r, w, g = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         used, peak = ctypes.c_size_t(), ctypes.c_size_t()
         _lib.raise_for(_lib.lib().ph_serve_stats(self._handle, ctypes.byref(q), ctypes.byref(r), ctypes.byref(used),
-                                                 ctypes.byref(peak), ctypes.byref(w)), self._ctx.handle)
+                                                 ctypes.byref(peak), ctypes.byref(w), ctypes.byref(g)),
+                       self._ctx.handle)
         return {"queued": q.value, "running": r.value, "bytes_in_use": used.value, "bytes_peak": peak.value,
-                "waited": w.value}
+                "waited": w.value, "grouped": g.value}
 
     def poll(self, ticket: int, wait: bool = False) -> float | None:
         lat = ctypes.c_double()

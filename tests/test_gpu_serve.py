@@ -136,3 +136,24 @@ def test_frame_ingest_equals_host_preprocessing(ph, cuda, channels, flip):
     from phtest import rel_l2, to_np
     assert rel_l2(to_np(proj), to_np(p_ref)) < 1e-6
     assert np.mean(to_np(arg) == to_np(a_ref)) > 0.999
+
+
+def test_same_shape_requests_share_launches(ph, cuda):
+    """Requests of one shape, slice count and optics that queue together are
+    admitted as a group on one slot and share one launch of each pass; every
+    result still equals its single call bit for bit."""
+    n, slices = 1024, 256
+    srv = ph.Server(max_shape=(n, n), max_slices=slices, lanes=1)
+    rng = np.random.default_rng(21)
+    holos = [to_dev(rng.uniform(0.1, 1.0, (n, n)).astype(np.float32), cuda) for _ in range(5)]
+    outs = [(torch.empty_like(h), torch.empty(h.shape, dtype=torch.int32, device=cuda)) for h in holos]
+    torch.cuda.synchronize()
+    tickets = [srv.submit(h, p, slices, 1500.0, 200.0, argmin=a) for h, (p, a) in zip(holos, outs)]
+    for t in tickets:
+        assert srv.poll(t, wait=True) > 0.0
+    st = srv.stats()
+    assert st["grouped"] >= 2, st                    # the ones queued behind the first ran as a group
+    for h, (p, a) in zip(holos, outs):
+        p1, a1 = _single(ph, h, slices, 1500.0, 200.0)
+        assert torch.equal(p, p1) and torch.equal(a, a1)
+    srv.close()
