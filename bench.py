@@ -347,6 +347,8 @@ def main():
     ap.add_argument("--no-standin", action="store_true", help="skip the cuFFT stand-in of the reference sequence")
     ap.add_argument("--no-forms", action="store_true", help="skip the tensor-core forms of the row pass")
     ap.add_argument("--no-extras", action="store_true", help="skip the brief batch (C4) and serving (C5) runs")
+    ap.add_argument("--shard", default="replica", choices=["replica", "depth"],
+                    help="replica: one frame per GPU; depth: one frame's slices split over the GPUs")
     ap.add_argument("--form", default="fp32", choices=["fp32", "bf16x3", "fp16x3", "fp16x2"],
                     help="arithmetic of the projection's row pass in the timed frames")
     args = ap.parse_args()
@@ -404,14 +406,29 @@ def main():
     stream = torch.cuda.current_stream(dev)
     s = stream.cuda_stream
 
+    depth = args.shard == "depth"
+    if depth:
+        # one frame over the ranks: GS replicated (each rank needs the whole field), the
+        # slices split into contiguous ranges with global indices, packed words merged
+        from ph_gb300 import parallel
+        k0, k1 = parallel.shard_range(S, rank, world)
+        packed = torch.empty((n, n), dtype=torch.int64, device=dev)
+
     def frame(in1, in2):
         if cfg["gs_iters"] > 0:
             ctx.call("ph_phase_retrieval", wf.data_ptr(), in1.data_ptr(), in2.data_ptr(), hp.data.data_ptr(),
                      hpi.data.data_ptr(), n, n, cfg["gs_iters"], None, s)
         else:
             ctx.call("ph_gabor_wavefront", wf.data_ptr(), in1.data_ptr(), n, n, s)
-        ctx.call("ph_reconst_xyproj", proj.data_ptr(), arg.data_ptr(), wf.data_ptr(), hf.data.data_ptr(),
-                 hdz.data.data_ptr(), n, n, S, s)
+        if depth:
+            ctx.call("ph_reconst_xyproj_range", packed.data_ptr(), wf.data_ptr(), hf.data.data_ptr(),
+                     hdz.data.data_ptr(), n, n, k0, k1, 0, s)
+            if world > 1:
+                dist.all_reduce(packed, op=dist.ReduceOp.MIN)
+            ctx.call("ph_unpack_projection", proj.data_ptr(), arg.data_ptr(), packed.data_ptr(), n, n, s)
+        else:
+            ctx.call("ph_reconst_xyproj", proj.data_ptr(), arg.data_ptr(), wf.data_ptr(), hf.data.data_ptr(),
+                     hdz.data.data_ptr(), n, n, S, s)
         ctx.call("ph_binarize_le", binary.data_ptr(), proj.data_ptr(), n * n, float(cfg["threshold"]), s)
         ctx.call("ph_ccl", labels.data_ptr(), binary.data_ptr(), _lib.PH_BOOL, n, n, s)
 
@@ -462,7 +479,8 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     total_ms = float(t.item())
     voxels = n * n * S
-    value = voxels * args.steps * world / (total_ms / 1e3) / 1e6
+    # replicas: every rank reconstructs its own frame; depth shards: the ranks share one frame
+    value = voxels * args.steps * (1 if depth else world) / (total_ms / 1e3) / 1e6
 
     # ---- end to end through the public API, host buffers
     e2e = None
@@ -477,7 +495,13 @@ def main():
                 u = ph.cu_phase_retrieval_holo(d1, d2, hp, hpi, cfg["gs_iters"], n)
             else:
                 u = ph.cu_gabor_wavefront(d1)
-            p, a = ph.cu_get_reconst_xyprojection(u, hf, hdz, S, return_argmin=True)
+            if depth:
+                pk = parallel.reconst_xyprojection_range(u, hf, hdz, k0, k1)
+                if world > 1:
+                    dist.all_reduce(pk, op=dist.ReduceOp.MIN)
+                p, a = parallel.unpack_projection(pk)
+            else:
+                p, a = ph.cu_get_reconst_xyprojection(u, hf, hdz, S, return_argmin=True)
             ctx.call("ph_binarize_le", binary.data_ptr(), p.data_ptr(), n * n, float(cfg["threshold"]), s)
             lab = ph.cu_connected_component_labeling(binary)
             proj_host.copy_(p, non_blocking=True)
@@ -500,7 +524,8 @@ def main():
         te = torch.tensor([sum(e_ms)], device=dev)
         if world > 1:
             dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        e2e = {"value": round(voxels * args.steps * world / (float(te.item()) / 1e3) / 1e6, 2), "unit": "Mvoxel/s",
+        e2e = {"value": round(voxels * args.steps * (1 if depth else world) / (float(te.item()) / 1e3) / 1e6, 2),
+               "unit": "Mvoxel/s",
                "h2d_bytes_per_step": int(h1.numel() * 4 * (2 if cfg["gs_iters"] > 0 else 1)),
                "d2h_bytes_per_step": int(proj.numel() * 4 + arg.numel() * 4 + 8),
                "p50_frame_ms": round(statistics.median(e_ms), 3),
@@ -611,7 +636,8 @@ def main():
     line = {
         "metric": "reconstructed Mvoxel/s + p99 frame latency, chosen vs plain FP32 form, 1 GB300",
         "value": round(value, 2), "unit": "Mvoxel/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "strong" if depth else "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded disc holograms generated on the device)",
         "config": {"workload": cfg["workload"], "n": n, "slices": S, "dz_um": cfg["dz"], "z0_um": cfg["z0"],
                    "gs_iterations": cfg["gs_iters"], "discs": cfg["discs"],
@@ -619,7 +645,8 @@ def main():
                    "l2": "flushed (512 MiB write) before every timed step",
                    "kernel_timing": f"{prof_steps} further steps with per-pass CUDA events on the launching stream "
                                     "(graph replay off); the frame time is taken without them",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+                   "parallelism": (f"depth shards x{world} (slice ranges, int64 MIN all-reduce of packed words)"
+                                   if depth else f"replicas x{world}" if world > 1 else "single GPU")},
         "p50_frame_ms": round(statistics.median(step_ms), 3),
         "p99_frame_ms": round(float(np.percentile(step_ms, 99)), 3),
         "gpu_launches": int(launches),
