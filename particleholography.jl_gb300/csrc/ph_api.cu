@@ -1152,13 +1152,13 @@ int issue_recon_group(ph_ctx *ctx, const std::vector<const ph_recon_item *> &its
     const int row_blocks_a = (nx + recon_a_rows(ny) - 1) / recon_a_rows(ny);
     const ph_tuning *tu = tuning_of(ctx, nx, ny);
     for (int k0 = 0; k0 < smax; k0 += L.batch) {
-        ReconA a{};
-        ReconB<EPI_PROJ> b{};
+        ReconAGrouped a{};
+        ReconB<EPI_PROJ, true> b{};
         for (int i = 0; i < G; ++i) {
             const int nb = std::max(0, std::min(L.batch, (int)its[i]->slices - k0));
             const int grp = nb > 0 ? recon_group(nb, row_blocks_a, recon_a_chain(ny), tu ? tu->group_cap : 0) : 1;
-            a.nb_items[i] = b.nb_items[i] = nb;
-            a.group_items[i] = b.group_items[i] = grp;
+            a.set_item(i, nb, grp);
+            b.set_item(i, nb, grp);
         }
         a.state = reinterpret_cast<const float4 *>(slot(0, L.state));
         a.t = reinterpret_cast<float2 *>(slot(0, L.t));
@@ -1169,26 +1169,26 @@ int issue_recon_group(ph_ctx *ctx, const std::vector<const ph_recon_item *> &its
         a.ny_out = ny;
         a.y0 = 0;
         a.k0 = k0;
-        a.nbatch = a.nb_items[0];   // item 0 has the most slices
-        a.group = a.group_items[0];
+        a.nbatch = a.item_nb(0);   // item 0 has the most slices
+        a.group = a.item_group(0);
         a.nitems = G;
         a.err = static_cast<int *>(ctx->small);
-        PH_TRY(pass(ctx, s, "recon_a", [&] { return launch_recon_a(ny, a, a.nbatch, s); }));
+        PH_TRY(pass(ctx, s, "recon_a", [&] { return launch_recon_a_group(ny, a, s); }));
         b.t = reinterpret_cast<const float2 *>(slot(0, L.t));
         b.tw = tw_x;
         b.proj64 = reinterpret_cast<unsigned long long *>(slot(0, L.p64));
-        b.t_stride = ib / sizeof(float2);
+        b.item_t_stride = ib / sizeof(float2);
         b.p64_stride = ib / sizeof(unsigned long long);
         b.rows = ny;
         b.nx_out = nx;
         b.x0 = 0;
         b.k0 = k0;
-        b.nbatch = b.nb_items[0];
-        b.group = b.group_items[0];
+        b.nbatch = b.item_nb(0);
+        b.group = b.item_group(0);
         b.vol_slice_stride = (long long)npix;
         b.nitems = G;
         b.err = static_cast<int *>(ctx->small);
-        PH_TRY(pass(ctx, s, "recon_b", [&] { return launch_recon_b(nx, b, s); }));
+        PH_TRY(pass(ctx, s, "recon_b", [&] { return launch_recon_b_group(nx, b, s); }));
     }
     for (int i = 0; i < G; ++i) {
         k_proj_finish<<<(unsigned)((npix + 255) / 256), 256, 0, s>>>(

@@ -22,10 +22,7 @@ bool recon_a_chain(int n) {
 }
 
 cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s) {
-    int gy = (nbatch + b.group - 1) / b.group;
-    for (int i = 0; b.nitems > 1 && i < b.nitems; ++i)
-        gy = std::max(gy, (b.nb_items[i] + b.group_items[i] - 1) / b.group_items[i]);
-    return launch_len<true>(n, b, b.nx, gy, s, b.nitems);
+    return launch_len<true>(n, b, b.nx, (nbatch + b.group - 1) / b.group, s);
 }
 
 }  // namespace ph

@@ -145,6 +145,8 @@ cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_SQRT_REAL> &b, cudaStream_
 cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_PADDED> &b, cudaStream_t s);
 cudaError_t launch_spectrum(int n, const SpectrumCols &b, cudaStream_t s);
 cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s);
+cudaError_t launch_recon_a_group(int n, const ReconAGrouped &b, cudaStream_t s);
+cudaError_t launch_recon_b_group(int n, const ReconB<EPI_PROJ, true> &b, cudaStream_t s);
 int recon_a_rows(int n);   // rows per pass A CTA for transform length n
 bool recon_a_chain(int n); // whether pass A at length n advances X by the product chain
 cudaError_t launch_recon_b(int n, const ReconB<EPI_PROJ> &b, cudaStream_t s);

@@ -23,6 +23,7 @@
 #pragma once
 
 #include <cuda_fp16.h>
+#include <type_traits>
 #include "ph_fft.cuh"
 #include "ph_tma.cuh"
 
@@ -152,10 +153,37 @@ __device__ __forceinline__ int shift_idx(int i, int n) {   // centred index of n
 // transform shape at once: blockIdx.z is the item.  Each item has its own
 // input and transfer functions (pointer tables in the pass's parameters), its
 // own slot of the scratch (the pass's pointers plus z times a stride) and its
-// own slice count within the batch (nb_items) and slices per CTA
-// (group_items), so every item is computed exactly as a single call would.
+// own slice count within the batch and slices per CTA
+// (its packed item word), so every item is computed exactly as a single call would.
 // With nitems = 1 (every single call) the tables are unused.
 constexpr int kMaxItems = 8;
+
+// The item tables of a grouped pass A / pass B, a base class of the grouped
+// instantiations only: the single-call kernels keep their parameters (and
+// their register allocation) unchanged.
+// Item z's slices in the batch and slices per CTA are packed into the 32-bit
+// halves of four 64-bit words (nb | group << 16) and selected without indexing
+// an array by blockIdx.z (which would copy the parameters to local memory).
+struct NoItems {};
+struct ReconItems {
+    int nitems = 1;
+    size_t item_state_stride = 0, item_t_stride = 0, p64_stride = 0;
+    unsigned long long item_words[kMaxItems / 2] = {};
+    __host__ void set_item(int z, int nb, int group) {
+        const unsigned long long w = (unsigned long long)((uint32_t)nb | ((uint32_t)group << 16));
+        item_words[z >> 1] = (item_words[z >> 1] & ~(0xFFFFFFFFull << ((z & 1) * 32))) | (w << ((z & 1) * 32));
+    }
+    __host__ __device__ int item_nb(int z) const { return (int)(word(z) & 0xFFFFu); }
+    __host__ __device__ int item_group(int z) const { return (int)(word(z) >> 16); }
+    __host__ __device__ uint32_t word(int z) const {
+        const unsigned long long a = (z >> 1) == 0 ? item_words[0]
+                                   : (z >> 1) == 1 ? item_words[1]
+                                   : (z >> 1) == 2 ? item_words[2]
+                                                   : item_words[3];
+        return (uint32_t)(a >> ((z & 1) * 32));
+    }
+};
+static_assert(kMaxItems == 8, "four packed words");
 
 // ---------------------------------------------------------------- forward rows (transposed store)
 
@@ -299,7 +327,8 @@ struct SpectrumCols : PassBase {
 // and after a cluster barrier each stores a 1 / (4 / ROWS) share of the y
 // range for all 4 rows, reading its peers' rows through distributed shared
 // memory.  (Stores of 2 consecutive kx, 16 bytes, ran 2-4x slower.)
-struct ReconA : PassBase {
+template <bool GROUPED = false>   // GROUPED: the grouped-launch form (grid z = item)
+struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
     // 4 rows of 128 threads at N = 2048: one CTA per SM.  (One row per CTA in
     // clusters of 4, or two in clusters of 2, measured 65 % / 59 % slower.)
     static constexpr int TT = 512;
@@ -314,9 +343,6 @@ struct ReconA : PassBase {
     int nx, ny_out, y0;
     int k0;                // global slice index of batch slot 0
     int nbatch, group;     // slices in the batch, slices per CTA
-    int nitems = 1;        // grouped launch: item z's state / t + z strides, its slices and group
-    size_t item_state_stride = 0, item_t_stride = 0;
-    int nb_items[kMaxItems] = {}, group_items[kMaxItems] = {};
 
     // Staged forms, the first that fits the CTA's shared memory beside the
     // exchange rows:
@@ -407,13 +433,21 @@ struct ReconA : PassBase {
         const int kx0 = (CS == 1 ? lin / gridDim.y : blockIdx.x) * ROWS;
         const int kx = kx0 + r;
         const bool valid = kx < nx;   // (CTAs that only pad a cluster hold no valid row)
-        const int z = blockIdx.z;
-        const int group = nitems > 1 ? group_items[z] : this->group;
+        // (the single-call form never touches the item tables: indexing them by
+        // blockIdx.z costs registers that the common path does not have)
+        int group = this->group, b1max = nbatch;
+        const float4 *state = this->state;
+        float2 *t = this->t;
+        if constexpr (GROUPED) {   // item z: its own slot of the scratch, slices and group
+            const int z = (int)blockIdx.z;
+            group = this->item_group(z);
+            b1max = this->item_nb(z);
+            state += (size_t)z * this->item_state_stride;
+            t += (size_t)z * this->item_t_stride;
+        }
         const int b0 = g * group;
-        const int b1 = min(b0 + group, nitems > 1 ? nb_items[z] : nbatch);
-        if (b0 >= b1) return;   // (an item with fewer slices; uniform over a cluster, which shares z and g)
-        const float4 *state = this->state + (size_t)z * item_state_stride;
-        float2 *t = this->t + (size_t)z * item_t_stride;
+        const int b1 = min(b0 + group, b1max);
+        if (GROUPED && b0 >= b1) return;   // (an item with fewer slices; uniform over a cluster: shared z and g)
         const float4 *srow = state + (size_t)(valid ? kx : 0) * N;
         float2 *xs = nullptr, *hs = nullptr;
         if constexpr (FORM == FORM_CHAIN) {
@@ -526,6 +560,9 @@ struct ReconA : PassBase {
     }
 };
 
+using ReconA = ReconAT<false>;
+using ReconAGrouped = ReconAT<true>;
+
 // ---------------------------------------------------------------- reconstruction pass B
 
 enum Epilogue {
@@ -553,8 +590,8 @@ __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f),
 // read it, the exchange rows of that slice's transform.  CTAs are small (128
 // threads: one row at N >= 2048) so that the barriers of the FFT stages span
 // only the warps that exchange data, and RTS / 128 CTAs share an SM.
-template <int EPI>
-struct ReconB : PassBase {
+template <int EPI, bool GROUPED = false>   // GROUPED: the grouped-launch form (EPI_PROJ, grid z = item)
+struct ReconB : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
     static constexpr int TT = 128;
     static constexpr int RTS = PH_RECONB_RTS;
     // 3 * 2^a lengths hold 24 values per thread and their running minima:
@@ -562,7 +599,7 @@ struct ReconB : PassBase {
     // 28 % faster than five CTAs at 96 registers (spilling ~480 bytes) and
     // 9-12 % faster than four at 128 (spilling ~150 bytes).
     template <int N>
-    static constexpr int rts() { return plan_pow2(N) ? RTS : 384; }
+    static constexpr int rts() { return plan_pow2(N) ? (GROUPED ? 512 : RTS) : 384; }   // (grouped: 128 registers, no spill)
     const float2 *t;                 // [batch][rows][nx]
     const float2 *tw;
     unsigned long long *proj64;      // [rows_out][nx_out] or null
@@ -577,9 +614,6 @@ struct ReconB : PassBase {
     int nx_out, x0;                  // stored columns [x0, x0 + nx_out)
     int k0, nbatch, group;
     long long vol_slice_stride;      // elements per stored slice
-    int nitems = 1;                  // grouped launch (EPI_PROJ): item z's t / proj64 + z strides, slices, group
-    size_t t_stride = 0, p64_stride = 0;
-    int nb_items[kMaxItems] = {}, group_items[kMaxItems] = {};
 
     // One buffer: the exchange rows (which also hold the dense bulk-copied rows).
     template <int N, bool RF>
@@ -607,13 +641,19 @@ struct ReconB : PassBase {
         const int yb = blockIdx.x * ROWS;
         const int y = yb + r;
         const bool valid = y < rows;
-        const int z = blockIdx.z;
-        const int group = nitems > 1 ? group_items[z] : this->group;
+        int group = this->group, b1max = nbatch;
+        const float2 *t = this->t;
+        unsigned long long *proj64 = this->proj64;
+        if constexpr (GROUPED) {   // item z: its own slot of the scratch, slices and group
+            const int z = (int)blockIdx.z;
+            group = this->item_group(z);
+            b1max = this->item_nb(z);
+            t += (size_t)z * this->item_t_stride;
+            proj64 += (size_t)z * this->p64_stride;
+        }
         const int b0 = blockIdx.y * group;
-        const int b1 = min(b0 + group, nitems > 1 ? nb_items[z] : nbatch);
-        if (b0 >= b1) return;   // (an item with fewer slices)
-        const float2 *t = this->t + (size_t)z * t_stride;
-        unsigned long long *proj64 = this->proj64 == nullptr ? nullptr : this->proj64 + (size_t)z * p64_stride;
+        const int b1 = min(b0 + group, b1max);
+        if (GROUPED && b0 >= b1) return;   // (an item with fewer slices)
         const int nvalid = min(ROWS, rows - yb);
         auto issue = [&](int b, int buf) {   // one thread: the rows of slice b into buffer buf
             fence_proxy_async_smem();

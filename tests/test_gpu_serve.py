@@ -143,7 +143,9 @@ def test_same_shape_requests_share_launches(ph, cuda):
     admitted as a group on one slot and share one launch of each pass; every
     result still equals its single call bit for bit."""
     n, slices = 1024, 256
-    srv = ph.Server(max_shape=(n, n), max_slices=slices, lanes=1)
+    block = _block_bytes(ph, cuda, n, slices)
+    # one slot, and a budget with room for several requests (the default pool holds one)
+    srv = ph.Server(max_shape=(n, n), max_slices=slices, lanes=1, budget_bytes=6 * block)
     rng = np.random.default_rng(21)
     holos = [to_dev(rng.uniform(0.1, 1.0, (n, n)).astype(np.float32), cuda) for _ in range(5)]
     outs = [(torch.empty_like(h), torch.empty(h.shape, dtype=torch.int32, device=cuda)) for h in holos]
