@@ -22,7 +22,7 @@ export cu_transfer_sqrt_arr, cu_transfer, cu_gabor_wavefront, cu_phase_retrieval
        cu_apply_low_pass_filter!, cu_apply_low_pass_filter,
        cu_rectangle_filter, cu_super_gaussian_filter, cu_get_reconst_xyprojection_lpf,
        cu_get_reconst_binary_vol, slice_bounding_rectangles, cu_reconst_subvolumes,
-       cu_make_background_mode, pad_with_mean,
+       cu_make_background_mode, pad_with_mean, autotune!,
        ReconBatch, run!, Server, submit!, poll
 
 const libphgb300 = get(ENV, "PHGB300_LIB", joinpath(@__DIR__, "..", "libphgb300.so"))
@@ -428,6 +428,24 @@ end
 function run!(b::ReconBatch)
     _check(ccall((:ph_batch_run, libphgb300), Int32, (Ptr{Cvoid}, Ptr{Cvoid}), b.handle, _stream()))
     return b.proj, b.argmin
+end
+
+"""New: times the reconstruction knobs of one shape once (slices per CTA, batch of
+intermediates and, with `allow_forms`, the split-precision row-pass forms) and
+keeps the fastest for later calls, batches and servers; `cache` is a JSON file
+keyed by device and shape.  Returns (form, group cap, batch slices, ms)."""
+function autotune!(n_fast::Int, n_slow::Int, slices::Int; allow_forms::Bool=false,
+                   cache::Union{Nothing,String}=nothing)
+    choice = zeros(Int32, 3)
+    ms = Ref{Float64}(0.0)
+    path = cache === nothing ? nothing : Base.cconvert(Cstring, cache)   # NUL-terminated, kept alive below
+    GC.@preserve path begin
+        _check(ccall((:ph_autotune, libphgb300), Int32,
+                     (Ptr{Cvoid}, Int32, Int32, Int32, Int32, Ptr{UInt8}, Ptr{Int32}, Ref{Float64}, Ptr{Cvoid}),
+                     _ctx(), n_fast, n_slow, slices, allow_forms ? Int32(1) : Int32(0),
+                     path === nothing ? Ptr{UInt8}(C_NULL) : pointer(path), choice, ms, _stream()))
+    end
+    return (Int(choice[1]), Int(choice[2]), Int(choice[3]), ms[])
 end
 
 # ph_serve_request (phgb300.h)
