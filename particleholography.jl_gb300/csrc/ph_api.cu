@@ -1961,9 +1961,21 @@ int32_t ph_batch_plan(ph_ctx *ctx, const ph_recon_item *items, int32_t count, in
     }
     // Groups: items of one transform shape and input kind, most slices first,
     // up to kMaxItems per group and kGroupBytes of scratch, share one launch
-    // of each pass.  (A shape whose projection runs a tensor-core row pass
-    // keeps one item per group: that pass has no grouped form.)
+    // of each pass.  Only items whose own pass A launch is small (under 4
+    // waves of CTAs) are grouped: a large item fills the GPU alone, and the
+    // grouped pass B runs fewer CTAs per SM.  (A shape whose projection runs a
+    // tensor-core row pass keeps one item per group: that pass has no grouped
+    // form.)
     constexpr size_t kGroupBytes = size_t(8) << 30;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess || sms <= 0) sms = 1;
+    auto small_item = [&](const ph_recon_item &it) {
+        const int rows_a = recon_a_rows(it.n_slow);
+        const long long blocks = (it.n_fast + rows_a - 1) / rows_a;
+        const int nb = std::min(it.slices, slice_batch(ctx, it.n_fast, it.n_slow, it.slices, kLaneBatchBytes));
+        const int grp = recon_group(nb, (int)blocks, recon_a_chain(it.n_slow));
+        return blocks * ((nb + grp - 1) / grp) < 4LL * sms;
+    };
     std::map<std::tuple<int, int, int>, std::vector<int>> classes;
     for (int i = 0; i < count; ++i)
         classes[{items[i].n_fast, items[i].n_slow, items[i].hologram != nullptr ? 1 : 0}].push_back(i);
@@ -1975,7 +1987,8 @@ int32_t ph_batch_plan(ph_ctx *ctx, const ph_recon_item *items, int32_t count, in
         const bool tc = effective_form(ctx, nx, ny) != PH_FORM_FP32;
         for (size_t k = 0; k < v.size();) {
             const size_t ib = group_item_bytes(ctx, nx, ny, items[v[k]].slices);
-            const size_t gmax = tc ? 1 : std::max<size_t>(1, std::min<size_t>(kMaxItems, kGroupBytes / ib));
+            const bool alone = tc || !small_item(items[v[k]]);
+            const size_t gmax = alone ? 1 : std::max<size_t>(1, std::min<size_t>(kMaxItems, kGroupBytes / ib));
             const size_t n = std::min(gmax, v.size() - k);
             groups.emplace_back(v.begin() + k, v.begin() + k + n);
             k += n;
