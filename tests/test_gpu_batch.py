@@ -59,8 +59,8 @@ def test_grouped_items_equal_single_calls(ph, cuda):
     so the product chains restart at the same slices)."""
     from ph_gb300 import _lib
     spec = [(256, 256, sl, True) for sl in (1, 5, 33, 64, 100, 7, 2, 200, 50, 3)]
-    spec += [(2048, 2048, sl, True) for sl in (96, 40, 200)]      # large: each alone
-    spec += [(2048, 2048, sl, True) for sl in (2, 1)]             # small launches: grouped, product chain
+    spec += [(2048, 2048, sl, True) for sl in (96, 40)]           # large launches: each alone
+    spec += [(512, 512, sl, True) for sl in (96, 40, 200, 3)]     # grouped, with pass A's product chain
     spec += [(1024, 512, sl, False) for sl in (12, 70, 1)]
     items = [_item(cuda, nx, ny, sl, seed=20 + i, as_hologram=h)[0] for i, (nx, ny, sl, h) in enumerate(spec)]
     ctx = _lib.default_context(0)
