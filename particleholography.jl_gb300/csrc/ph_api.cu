@@ -907,6 +907,38 @@ int recon_group(int nbatch, int nx_rows_a, bool chain, int cap_override = 0) {
     return std::max(1, std::min(cap, nbatch / groups));
 }
 
+// cuTensorMapEncodeTiled, looked up through the runtime's driver entry point
+// (the library does not link the driver library); null if unavailable.
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// Tensor map of the slice intermediate T = [nb][ny_out][nx] float2 (8-byte
+// elements) for pass A's tiled store: boxes of 4 kx x 256 y x 1 slice.
+bool t_store_map(CUtensorMap *tm, float2 *t, int nx, int ny_out, int nb) {
+    const EncodeTiledFn enc = encode_tiled();
+    if (enc == nullptr || ((uintptr_t)t & 15) != 0 || nx % 4 != 0) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny_out, (cuuint64_t)nb};
+    const cuuint64_t strides[2] = {(cuuint64_t)nx * 8, (cuuint64_t)nx * ny_out * 8};
+    const cuuint32_t box[3] = {4, (cuuint32_t)ReconATStore::kBoxY, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return enc(tm, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, t, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // The slice loop of a reconstruction: pass A and pass B per batch, then the
 // projection unpacking.
 int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype, int nx,
@@ -920,18 +952,28 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
         const int nb = std::min(L.batch, first + slices - k0);
         const ph_tuning *tu = tuning_of(ctx, nx, ny);
         const int group = recon_group(nb, row_blocks_a, recon_a_chain(ny), tu ? tu->group_cap : 0);
-        ReconA a{};
-        a.state = state;
-        a.t = t;
-        a.tw = tw_y;
-        a.nx = nx;
-        a.ny_out = ny_out;
-        a.y0 = y0;
-        a.k0 = k0;
-        a.nbatch = nb;
-        a.group = group;
-        a.err = static_cast<int *>(ctx->small);
-        PH_TRY(pass(ctx, s, "recon_a",[&] { return launch_recon_a(ny, a, nb, s); }));
+        const auto fill_a = [&](auto &a) {
+            a.state = state;
+            a.t = t;
+            a.tw = tw_y;
+            a.nx = nx;
+            a.ny_out = ny_out;
+            a.y0 = y0;
+            a.k0 = k0;
+            a.nbatch = nb;
+            a.group = group;
+            a.err = static_cast<int *>(ctx->small);
+        };
+        CUtensorMap tm;
+        if (recon_a_tstore(ny) && y0 == 0 && ny_out == ny && t_store_map(&tm, t, nx, ny_out, nb)) {
+            ReconATStore a{};
+            fill_a(a);
+            PH_TRY(pass(ctx, s, "recon_a", [&] { return launch_recon_a_tstore(ny, a, tm, nb, s); }));
+        } else {
+            ReconA a{};
+            fill_a(a);
+            PH_TRY(pass(ctx, s, "recon_a", [&] { return launch_recon_a(ny, a, nb, s); }));
+        }
         if (kind == RK_PROJ && effective_form(ctx, nx, ny) != PH_FORM_FP32) {
             const int form = effective_form(ctx, nx, ny);
             ReconBTc b{};

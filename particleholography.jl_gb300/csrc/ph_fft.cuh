@@ -169,7 +169,11 @@ struct RowSync {
 //   OUT_SMEM: write the outputs to srow (after an internal barrier) and call
 //             store() first so it may transform the value; ends with a barrier.
 //             store() must then RETURN the value to write: float2 store(slot, col, v).
-template <int N, int E, bool INV, bool OUT_SMEM = false, class Tw, class Load, class Store, class Sync>
+//   STORE_SYNC: (without OUT_SMEM) a barrier between the last stage's reads of
+//             srow and the store() calls, which may then write shared memory
+//             that other threads' last-stage inputs occupied.
+template <int N, int E, bool INV, bool OUT_SMEM = false, bool STORE_SYNC = false, class Tw, class Load,
+          class Store, class Sync>
 __device__ __forceinline__ void fft_row_sync(float2 *__restrict__ srow, int j, const Tw tw, Load &&load,
                                              Store &&store, const Sync &sync) {
     using PL = FftPlan<N, E>;
@@ -234,6 +238,7 @@ __device__ __forceinline__ void fft_row_sync(float2 *__restrict__ srow, int j, c
             }
             // ---- scatter outputs
             if constexpr (LASTSTAGE && !OUT_SMEM) {
+                if constexpr (STORE_SYNC) sync();
 #pragma unroll
                 for (int m = 0; m < M; ++m) {
                     const int b = j + m * P;   // last stage: (b / NS) == 0, out = b + r*NS

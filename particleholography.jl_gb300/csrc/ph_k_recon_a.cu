@@ -25,4 +25,11 @@ cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s) {
     return launch_len<true>(n, b, b.nx, (nbatch + b.group - 1) / b.group, s);
 }
 
+bool recon_a_tstore(int n) { return n == 2048; }
+
+cudaError_t launch_recon_a_tstore(int n, const ReconATStore &b, const CUtensorMap &tm, int nbatch, cudaStream_t s) {
+    if (n != 2048) return cudaErrorInvalidValue;
+    return launch_one_tm<2048, true>(b, tm, b.nx, (nbatch + b.group - 1) / b.group, s);
+}
+
 }  // namespace ph

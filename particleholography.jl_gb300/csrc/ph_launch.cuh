@@ -103,6 +103,32 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s, 
     return cudaGetLastError();
 }
 
+// A plain (no cluster, no programmatic dependency) launch of k_pass_tm.
+template <int N, bool ROW_FAST, class Body>
+cudaError_t launch_one_tm(const Body &body, const CUtensorMap &tm, int nrows, int grid_y, cudaStream_t s) {
+    auto kern = k_pass_tm<N, ROW_FAST, Body>;
+    constexpr size_t smem = Body::template smem<N, ROW_FAST>();
+    static_assert(smem <= kSmemMax, "pass needs more shared memory than a CTA has");
+    static_assert(Body::template cluster<N>() == 1 && !Body::template pdl<N>() && !Body::template persistent<N>(),
+                  "plain launches only");
+    if constexpr (smem > 48 * 1024) {
+        static unsigned long long done_mask = 0;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const unsigned long long bit = 1ull << (dev & 63);
+        if (!(__atomic_load_n(&done_mask, __ATOMIC_ACQUIRE) & bit)) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            __atomic_fetch_or(&done_mask, bit, __ATOMIC_ACQ_REL);
+        }
+    }
+    using S = Shape<N, Body::EPT, Body::TT>;
+    const int gx = (nrows + S::ROWS - 1) / S::ROWS;
+    if (gx == 0) return cudaSuccess;
+    kern<<<dim3(gx, grid_y), S::THREADS, smem, s>>>(body, tm);
+    return cudaGetLastError();
+}
+
 // Launch of a pass that exists only for the lengths where Body::staged<N>() holds.
 template <bool ROW_FAST, class Body>
 cudaError_t launch_staged_len(int n, const Body &body, int nrows, cudaStream_t s) {
@@ -145,6 +171,10 @@ cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_SQRT_REAL> &b, cudaStream_
 cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_PADDED> &b, cudaStream_t s);
 cudaError_t launch_spectrum(int n, const SpectrumCols &b, cudaStream_t s);
 cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s);
+// Pass A with the tensor-map transposed store (lengths where recon_a_tstore holds;
+// tm: T as [nbatch][ny_out = n][nx] 8-byte elements, boxes of 4 x 256 x 1).
+bool recon_a_tstore(int n);
+cudaError_t launch_recon_a_tstore(int n, const ReconATStore &b, const CUtensorMap &tm, int nbatch, cudaStream_t s);
 cudaError_t launch_recon_a_group(int n, const ReconAGrouped &b, cudaStream_t s);
 cudaError_t launch_recon_b_group(int n, const ReconB<EPI_PROJ, true> &b, cudaStream_t s);
 int recon_a_rows(int n);   // rows per pass A CTA for transform length n

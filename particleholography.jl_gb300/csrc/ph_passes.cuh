@@ -142,6 +142,19 @@ __global__ void __launch_bounds__(Shape<N, Body::EPT, Body::TT>::THREADS, min_bl
     body.template run<N, ROW_FAST>(ph_smem, r, j);
 }
 
+// A pass whose body also takes a tensor map.  The map is a __grid_constant__
+// parameter of its own (the copy engine reads it where the kernel's
+// parameters live); the body stays an ordinary parameter.
+template <int N, bool ROW_FAST, class Body>
+__global__ void __launch_bounds__(Shape<N, Body::EPT, Body::TT>::THREADS, min_blocks<N, Body>())
+    k_pass_tm(const Body body, const __grid_constant__ CUtensorMap tm) {
+    extern __shared__ __align__(128) unsigned char ph_smem[];
+    const int t = threadIdx.x;
+    const int r = ThreadMap<N, Body::EPT, Body::TT, ROW_FAST>::row(t);
+    const int j = ThreadMap<N, Body::EPT, Body::TT, ROW_FAST>::j(t);
+    body.template run<N, ROW_FAST>(ph_smem, r, j, &tm);
+}
+
 __device__ __forceinline__ int shift_idx(int i, int n) {   // centred index of natural frequency i
     int s = i + (n >> 1);
     return s >= n ? s - n : s;
@@ -327,7 +340,7 @@ struct SpectrumCols : PassBase {
 // and after a cluster barrier each stores a 1 / (4 / ROWS) share of the y
 // range for all 4 rows, reading its peers' rows through distributed shared
 // memory.  (Stores of 2 consecutive kx, 16 bytes, ran 2-4x slower.)
-template <bool GROUPED = false>   // GROUPED: the grouped-launch form (grid z = item)
+template <bool GROUPED = false, bool TSTORE = false>   // GROUPED: the grouped-launch form (grid z = item)
 struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
     // 4 rows of 128 threads at N = 2048: one CTA per SM.  (One row per CTA in
     // clusters of 4, or two in clusters of 2, measured 65 % / 59 % slower.)
@@ -418,11 +431,24 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
         return cmul(make_float2(s.x, s.y), make_float2(cs * mag, sn * mag));
     }
 
+    // TSTORE: the transposed store through a tensor map.  The last stage
+    // writes the CTA's 4 rows to shared memory as [y][kx mod 4] (over the
+    // exchange rows, after a barrier), and one thread stores them in boxes of
+    // 4 kx x 256 y: the LSU no longer carries 8 sectors of 8 different lines
+    // per warp store.  Full-size frames only (y0 = 0, ny_out = N, nx a
+    // multiple of 4), lengths 256 .. 2048 (one CTA holds 4 rows).
+    static constexpr int kBoxY = 256;
+    template <int N>
+    static constexpr bool tstore_ok() {
+        return Shape<N, EPT, TT>::ROWS == 4 && N >= kBoxY && cluster<N>() == 1;
+    }
+
     template <int N, bool RF>
-    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j, const void *tmap = nullptr) const {
         using S = Shape<N, EPT, TT>;
         constexpr int ROWS = S::ROWS;
         constexpr int FORM = form<N, RF>();
+        static_assert(!TSTORE || tstore_ok<N>(), "tensor-map store: 4 rows per CTA, N >= 256");
         unsigned char *xbase = smem + stage_total<N, RF>();
         constexpr int CS = cluster<N>();
         // The CTAs of one row block (its `gridDim.y` slice groups) are consecutive
@@ -513,7 +539,30 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
                     return direct(srow[ky], k);
                 }
             };
-            if constexpr (CS == 1) {
+            if constexpr (TSTORE) {
+                float2 *stg = reinterpret_cast<float2 *>(xbase);   // [y][ROWS], over the exchange rows
+                int nsync = 0;
+                // The first barrier of the transform precedes its first exchange
+                // write: the previous slice's boxes must have left the staging.
+                const auto sync = [&nsync]() {
+                    if (nsync++ == 0 && threadIdx.x == 0) bulk_wait_read_all();
+                    __syncthreads();
+                };
+                fft_row_sync<N, S::E, true, false, true>(
+                    xr, j, tw, load, [&](int, int y, float2 v) { stg[y * ROWS + r] = v; }, sync);
+                fence_proxy_async_smem();   // the staging writes, before the copy engine reads them
+                if (threadIdx.x < 32) {
+                    named_bar_sync(1, S::THREADS);
+                    if (threadIdx.x == 0) {
+#pragma unroll 1
+                        for (int q = 0; q < N / kBoxY; ++q)
+                            tma_store_3d(tmap, stg + (size_t)q * kBoxY * ROWS, kx0, q * kBoxY, b);
+                        bulk_commit();
+                    }
+                } else {
+                    named_bar_arrive(1, S::THREADS);
+                }
+            } else if constexpr (CS == 1) {
                 fft_row<N, S::E, true>(xr, j, tw, load, [&](int, int y, float2 v) {
                     const int yo = y - y0;
                     // streaming store: T passes through L2 once
@@ -557,10 +606,14 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
             }
         }
         if constexpr (CS > 1) cluster_wait();   // no CTA leaves while a peer reads its rows
+        if constexpr (TSTORE) {
+            if (threadIdx.x == 0) bulk_wait_all();   // the shared memory outlives the last boxes' reads
+        }
     }
 };
 
 using ReconA = ReconAT<false>;
+using ReconATStore = ReconAT<false, true>;
 using ReconAGrouped = ReconAT<true>;
 
 // ---------------------------------------------------------------- reconstruction pass B

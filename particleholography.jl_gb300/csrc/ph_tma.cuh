@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>   // CUtensorMap (the type only: maps are encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 namespace ph {
@@ -132,6 +133,31 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
             smem_addr(dst)),
         "l"(src), "r"(bytes), "r"(smem_addr(bar))
         : "memory");
+}
+
+// ---- tiled bulk stores (shared -> global through a tensor map)
+
+// One box of a 3-D tensor map from shared memory (128-byte aligned) to the
+// tensor at element coordinates (x, y, z); x times the element size must be a
+// multiple of 16 bytes and no coordinate negative.  Elements outside the
+// tensor are not written.  The issuing thread tracks it in its bulk group.
+__device__ __forceinline__ void tma_store_3d(const void *tmap, const void *src, int x, int y, int z) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(tmap),
+                 "r"(smem_addr(src)), "r"(x), "r"(y), "r"(z)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// The issuing thread's committed bulk stores have read their shared-memory source.
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// ... and have completed.
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// Named barriers: `count` threads (a multiple of 32) take part; arrive does not wait.
+__device__ __forceinline__ void named_bar_sync(int id, int count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void named_bar_arrive(int id, int count) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
 }  // namespace ph
