@@ -25,11 +25,16 @@ cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s) {
     return launch_len<true>(n, b, b.nx, (nbatch + b.group - 1) / b.group, s);
 }
 
-bool recon_a_tstore(int n) { return n == 2048; }
+// The tensor-map form: 4-row CTAs at 2048, clusters of two 2-row CTAs at 4096.
+bool recon_a_tstore(int n) { return n == 2048 || n == 4096; }
 
 cudaError_t launch_recon_a_tstore(int n, const ReconATStore &b, const CUtensorMap &tm, int nbatch, cudaStream_t s) {
-    if (n != 2048) return cudaErrorInvalidValue;
-    return launch_one_tm<2048, true>(b, tm, b.nx, (nbatch + b.group - 1) / b.group, s);
+    const int gy = (nbatch + b.group - 1) / b.group;
+    switch (n) {
+        case 2048: return launch_one_tm<2048, true>(b, tm, b.nx, gy, s);
+        case 4096: return launch_one_tm<4096, true>(b, tm, b.nx, gy, s);
+    }
+    return cudaErrorInvalidValue;
 }
 
 }  // namespace ph

@@ -103,14 +103,14 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s, 
     return cudaGetLastError();
 }
 
-// A plain (no cluster, no programmatic dependency) launch of k_pass_tm.
+// A launch of k_pass_tm (clusters of Body::cluster<N>() CTAs; no programmatic
+// dependency, not persistent).
 template <int N, bool ROW_FAST, class Body>
 cudaError_t launch_one_tm(const Body &body, const CUtensorMap &tm, int nrows, int grid_y, cudaStream_t s) {
     auto kern = k_pass_tm<N, ROW_FAST, Body>;
     constexpr size_t smem = Body::template smem<N, ROW_FAST>();
     static_assert(smem <= kSmemMax, "pass needs more shared memory than a CTA has");
-    static_assert(Body::template cluster<N>() == 1 && !Body::template pdl<N>() && !Body::template persistent<N>(),
-                  "plain launches only");
+    static_assert(!Body::template pdl<N>() && !Body::template persistent<N>(), "plain or cluster launches only");
     if constexpr (smem > 48 * 1024) {
         static unsigned long long done_mask = 0;
         int dev = 0;
@@ -125,6 +125,22 @@ cudaError_t launch_one_tm(const Body &body, const CUtensorMap &tm, int nrows, in
     using S = Shape<N, Body::EPT, Body::TT>;
     const int gx = (nrows + S::ROWS - 1) / S::ROWS;
     if (gx == 0) return cudaSuccess;
+    constexpr int CS = Body::template cluster<N>();
+    if constexpr (CS > 1) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((gx + CS - 1) / CS * CS, grid_y, 1);
+        cfg.blockDim = dim3(S::THREADS);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = CS;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, kern, body, tm);
+    }
     kern<<<dim3(gx, grid_y), S::THREADS, smem, s>>>(body, tm);
     return cudaGetLastError();
 }

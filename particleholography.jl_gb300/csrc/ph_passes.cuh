@@ -431,16 +431,24 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
         return cmul(make_float2(s.x, s.y), make_float2(cs * mag, sn * mag));
     }
 
-    // TSTORE: the transposed store through a tensor map.  The last stage
-    // writes the CTA's 4 rows to shared memory as [y][kx mod 4] (over the
-    // exchange rows, after a barrier), and one thread stores them in boxes of
-    // 4 kx x 256 y: the LSU no longer carries 8 sectors of 8 different lines
-    // per warp store.  Full-size frames only (y0 = 0, ny_out = N, nx a
-    // multiple of 4), lengths 256 .. 2048 (one CTA holds 4 rows).
+    // TSTORE: the transposed store through a tensor map, in boxes of 4 kx x
+    // 256 y (whole 32-byte sectors: boxes of 2 kx, 16-byte halves, measured
+    // 2-5x slower).  The last stage writes the 4 rows of kx to shared memory
+    // as [y][kx mod 4] (over the exchange rows, after a barrier) and one
+    // thread stores the boxes: the LSU no longer carries 8 sectors of 8
+    // different lines per warp store.
+    //  - 4 rows per CTA: the CTA stages and stores all y.
+    //  - 2 rows per CTA, clusters of 2: CTA c stages y in [c N/2, (c+1) N/2)
+    //    of all 4 rows; each CTA writes its outputs into the owner's staging
+    //    (distributed shared memory for the peer's half) between two cluster
+    //    barriers (the owner's last-stage reads are done; the writes are
+    //    complete), then each stores its half.
+    // Full-size frames only (y0 = 0, ny_out = N, nx a multiple of 4).
     static constexpr int kBoxY = 256;
     template <int N>
     static constexpr bool tstore_ok() {
-        return Shape<N, EPT, TT>::ROWS == 4 && N >= kBoxY && cluster<N>() == 1;
+        constexpr int R = Shape<N, EPT, TT>::ROWS;
+        return N >= 2 * kBoxY && ((R == 4 && cluster<N>() == 1) || (R == 2 && cluster<N>() == 2));
     }
 
     template <int N, bool RF>
@@ -448,7 +456,7 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
         using S = Shape<N, EPT, TT>;
         constexpr int ROWS = S::ROWS;
         constexpr int FORM = form<N, RF>();
-        static_assert(!TSTORE || tstore_ok<N>(), "tensor-map store: 4 rows per CTA, N >= 256");
+        static_assert(!TSTORE || tstore_ok<N>(), "tensor-map store: 4 rows per CTA or 2 in a cluster of 2, N >= 512");
         unsigned char *xbase = smem + stage_total<N, RF>();
         constexpr int CS = cluster<N>();
         // The CTAs of one row block (its `gridDim.y` slice groups) are consecutive
@@ -522,7 +530,7 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
             srow = reinterpret_cast<const float4 *>(smem + (size_t)r * SS);
         }
         float2 *xr = xrow<N, EPT, TT, RF>(xbase, r);
-        if constexpr (CS > 1) cluster_arrive_relaxed();   // pairs with the first slice's wait
+        if constexpr (CS > 1 && !TSTORE) cluster_arrive_relaxed();   // pairs with the first slice's wait
         for (int b = b0; b < b1; ++b) {
             const uint32_t k = (uint32_t)(k0 + b);
             float2 *tb = t + (size_t)b * ny_out * nx;
@@ -539,7 +547,48 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
                     return direct(srow[ky], k);
                 }
             };
-            if constexpr (TSTORE) {
+            if constexpr (TSTORE && CS == 2) {
+                // stg: [y - rank N/2][4] for this CTA's half of y, over the exchange rows
+                constexpr int YH = N / 2;
+                constexpr int LAST_SYNC = 2 * (FftPlan<N, S::E>::NSTAGES - 1);   // the one before store()
+                const uint32_t rank = cluster_ctarank();
+                const uint32_t stg_own = smem_addr(xbase);
+                const uint32_t stg_peer = map_to_rank(stg_own, rank ^ 1u);
+                int nsync = 0;
+                // First barrier: the previous slice's boxes have left the
+                // staging.  Last: both CTAs have read their last stage's
+                // inputs, so the staging (the peer's included) may be written.
+                const auto sync = [&nsync]() {
+                    const int i = nsync++;
+                    if (i == 0 && threadIdx.x == 0) bulk_wait_read_all();
+                    if (i == LAST_SYNC) {
+                        cluster_sync();
+                    } else {
+                        __syncthreads();
+                    }
+                };
+                fft_row_sync<N, S::E, true, false, true>(
+                    xr, j, tw, load,
+                    [&](int, int y, float2 v) {
+                        const uint32_t owner = (uint32_t)(y / YH);
+                        const uint32_t off = (uint32_t)((((y % YH) * 4) + (int)rank * ROWS + r) * 8);
+                        if (owner == rank) {
+                            st_shared_f2(stg_own + off, v);
+                        } else {
+                            st_cluster_f2(stg_peer + off, v);
+                        }
+                    },
+                    sync);
+                fence_proxy_async_cluster();   // the staging writes (local and remote), before the copy engine reads them
+                cluster_sync();                // every write into this CTA's staging has landed
+                if (threadIdx.x == 0) {
+#pragma unroll 1
+                    for (int q = 0; q < YH / kBoxY; ++q)
+                        tma_store_3d(tmap, reinterpret_cast<const float2 *>(xbase) + (size_t)q * kBoxY * 4,
+                                     kx0 - (int)rank * ROWS, (int)rank * YH + q * kBoxY, b);
+                    bulk_commit();
+                }
+            } else if constexpr (TSTORE) {
                 float2 *stg = reinterpret_cast<float2 *>(xbase);   // [y][ROWS], over the exchange rows
                 int nsync = 0;
                 // The first barrier of the transform precedes its first exchange
@@ -605,7 +654,7 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
                 cluster_arrive_relaxed();
             }
         }
-        if constexpr (CS > 1) cluster_wait();   // no CTA leaves while a peer reads its rows
+        if constexpr (CS > 1 && !TSTORE) cluster_wait();   // no CTA leaves while a peer reads its rows
         if constexpr (TSTORE) {
             if (threadIdx.x == 0) bulk_wait_all();   // the shared memory outlives the last boxes' reads
         }
