@@ -939,6 +939,20 @@ bool t_store_map(CUtensorMap *tm, float2 *t, int nx, int ny_out, int nb) {
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Tensor map of a [outer][inner] float2 array for the persistent GS passes'
+// tiled store: boxes of `rows` (along inner) x kGsBox (along outer).
+bool gs_store_map(CUtensorMap *tm, float2 *p, int inner, int outer, int rows) {
+    const EncodeTiledFn enc = encode_tiled();
+    if (enc == nullptr || ((uintptr_t)p & 15) != 0 || inner % 4 != 0 || rows <= 0) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)outer};
+    const cuuint64_t strides[1] = {(cuuint64_t)inner * 8};
+    const cuuint32_t box[2] = {(cuuint32_t)rows, (cuuint32_t)kGsBox};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(tm, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, p, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // The slice loop of a reconstruction: pass A and pass B per batch, then the
 // projection unpacking.
 int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype, int nx,
@@ -1527,21 +1541,32 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
     f.tw = tw_x;
     f.nrows = ny;
     PH_TRY(pass(ctx, s, "fwd_rows",[&] { return launch_fwd_rows(nx, f, s); }));
+    // The staged passes store through tensor maps where their blocks allow it:
+    // the column pass writes bufb = [ny][nx], the row pass bufa = [nx][ny].
+    CUtensorMap tm_col, tm_row;
+    const bool ts_col = staged && gs_tstore_len(ny) && gs_store_map(&tm_col, bufb, nx, ny, gs_rows(ny));
+    const bool ts_row = staged && gs_tstore_len(nx) && gs_store_map(&tm_row, bufa, ny, nx, gs_rows(nx));
+    const auto col = [&](const GsColT &c) {
+        return ts_col ? launch_gs_col_ts(ny, c, tm_col, s) : launch_gs_col_t(ny, c, s);
+    };
+    const auto row = [&](const GsRowMidT &r) {
+        return ts_row ? launch_gs_row_ts(nx, r, tm_row, s) : launch_gs_row_t(nx, r, s);
+    };
     for (int it = 0; it < priter && staged; ++it) {
         const bool last = it == priter - 1;
         GsColT c{};
         c.src = bufa; c.ht = ht; c.dst = bufb; c.tw = tw_y; c.err = err; c.nx = nx;
-        PH_TRY(pass(ctx, s, "gs_col",[&] { return launch_gs_col_t(ny, c, s); }));
+        PH_TRY(pass(ctx, s, "gs_col",[&] { return col(c); }));
         GsRowMidT r2{};
         r2.src = bufb; r2.holo = amp2; r2.dst = bufa; r2.tw = tw_x; r2.err = err; r2.nrows = ny;
         r2.resid = (last && residual) ? acc : nullptr;
-        PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return launch_gs_row_t(nx, r2, s); }));
+        PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return row(r2); }));
         c.src = bufa; c.ht = hti; c.dst = bufb;
-        PH_TRY(pass(ctx, s, "gs_col",[&] { return launch_gs_col_t(ny, c, s); }));
+        PH_TRY(pass(ctx, s, "gs_col",[&] { return col(c); }));
         if (!last) {
             GsRowMidT r1{};
             r1.src = bufb; r1.holo = amp1; r1.dst = bufa; r1.tw = tw_x; r1.err = err; r1.nrows = ny;
-            PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return launch_gs_row_t(nx, r1, s); }));
+            PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return row(r1); }));
         } else {
             GsRow<ROW_FINAL> r1{};
             r1.src = bufb; r1.holo = holo1; r1.dst = o; r1.tw = tw_x; r1.nrows = ny;

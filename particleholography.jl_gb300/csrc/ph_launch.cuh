@@ -103,14 +103,14 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s, 
     return cudaGetLastError();
 }
 
-// A launch of k_pass_tm (clusters of Body::cluster<N>() CTAs; no programmatic
-// dependency, not persistent).
+// A launch of k_pass_tm: the body and a tensor map (clusters of
+// Body::cluster<N>() CTAs, persistent grids and programmatic dependents as in
+// launch_one).
 template <int N, bool ROW_FAST, class Body>
 cudaError_t launch_one_tm(const Body &body, const CUtensorMap &tm, int nrows, int grid_y, cudaStream_t s) {
     auto kern = k_pass_tm<N, ROW_FAST, Body>;
     constexpr size_t smem = Body::template smem<N, ROW_FAST>();
     static_assert(smem <= kSmemMax, "pass needs more shared memory than a CTA has");
-    static_assert(!Body::template pdl<N>() && !Body::template persistent<N>(), "plain or cluster launches only");
     if constexpr (smem > 48 * 1024) {
         static unsigned long long done_mask = 0;
         int dev = 0;
@@ -123,26 +123,46 @@ cudaError_t launch_one_tm(const Body &body, const CUtensorMap &tm, int nrows, in
         }
     }
     using S = Shape<N, Body::EPT, Body::TT>;
-    const int gx = (nrows + S::ROWS - 1) / S::ROWS;
+    int gx = (nrows + S::ROWS - 1) / S::ROWS;
+    if constexpr (Body::template persistent<N>()) {
+        static int slots[64] = {};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        int c = __atomic_load_n(&slots[dev & 63], __ATOMIC_ACQUIRE);
+        if (c == 0) {
+            int per_sm = 0, sms = 0;
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, S::THREADS, smem);
+            if (e != cudaSuccess) return e;
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (e != cudaSuccess) return e;
+            c = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+            __atomic_store_n(&slots[dev & 63], c, __ATOMIC_RELEASE);
+        }
+        gx = gx < c ? gx : c;
+    }
     if (gx == 0) return cudaSuccess;
     constexpr int CS = Body::template cluster<N>();
+    static_assert(CS == 1 || !Body::template pdl<N>(), "cluster or programmatic-dependent launch, not both");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((gx + CS - 1) / CS * CS, grid_y, 1);
+    cfg.blockDim = dim3(S::THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
     if constexpr (CS > 1) {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((gx + CS - 1) / CS * CS, grid_y, 1);
-        cfg.blockDim = dim3(S::THREADS);
-        cfg.dynamicSmemBytes = smem;
-        cfg.stream = s;
-        cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeClusterDimension;
         attr[0].val.clusterDim.x = CS;
         attr[0].val.clusterDim.y = 1;
         attr[0].val.clusterDim.z = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, kern, body, tm);
+    } else if constexpr (Body::template pdl<N>()) {
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
     }
-    kern<<<dim3(gx, grid_y), S::THREADS, smem, s>>>(body, tm);
-    return cudaGetLastError();
+    return cudaLaunchKernelEx(&cfg, kern, body, tm);
 }
 
 // Launch of a pass that exists only for the lengths where Body::staged<N>() holds.
@@ -192,6 +212,13 @@ cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s);
 bool recon_a_tstore(int n);
 cudaError_t launch_recon_a_tstore(int n, const ReconATStore &b, const CUtensorMap &tm, int nbatch, cudaStream_t s);
 cudaError_t launch_recon_a_group(int n, const ReconAGrouped &b, cudaStream_t s);
+// The persistent GS passes with the tensor-map store (lengths where
+// gs_tstore_len holds; tm: dst as a 2-D tensor of 8-byte elements, inner
+// dimension the rows' index, boxes of rows-per-block x 256).
+bool gs_tstore_len(int n);
+int gs_rows(int n);   // rows per block of the persistent GS passes
+cudaError_t launch_gs_col_ts(int n, const GsColT &b, const CUtensorMap &tm, cudaStream_t s);
+cudaError_t launch_gs_row_ts(int n, const GsRowMidT &b, const CUtensorMap &tm, cudaStream_t s);
 cudaError_t launch_recon_b_group(int n, const ReconB<EPI_PROJ, true> &b, cudaStream_t s);
 int recon_a_rows(int n);   // rows per pass A CTA for transform length n
 bool recon_a_chain(int n); // whether pass A at length n advances X by the product chain

@@ -871,6 +871,15 @@ struct ReconB : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
 
 // ---------------------------------------------------------------- Gerchberg-Saxton / propagation
 
+// Tensor-map stores of the persistent GS passes: boxes of ROWS x kGsBox,
+// where a block holds 4 or 8 rows (whole 32-byte sectors or two) and the
+// transform length is a multiple of kGsBox.
+constexpr int kGsBox = 256;
+template <int N>
+constexpr bool gs_tstore_ok() {
+    return (Shape<N>::ROWS == 4 || Shape<N>::ROWS == 8) && N % kGsBox == 0;
+}
+
 enum RowMode {
     ROW_MID = 0,      // inverse FFT -> amplitude replace -> forward FFT -> transposed store
     ROW_FINAL = 1,    // inverse FFT -> amplitude replace -> natural store
@@ -1052,11 +1061,16 @@ struct GsRowMidT : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        run_blocks<N, RF, false>(smem, r, j);
+        run_blocks<N, RF, false, false>(smem, r, j, nullptr);
     }
 
-    template <int N, bool RF, bool RESID>
-    __device__ __forceinline__ void run_blocks(unsigned char *smem, int r, int j) const {
+    // The transposed store through a tensor map (gs_tstore_ok: 4 or 8 rows
+    // per block, N a multiple of 256): the forward transform's outputs are
+    // staged as [kx][y mod ROWS] over the block's field rows and one thread
+    // stores them in boxes of ROWS y x 256 kx (whole 32-byte sectors), as in
+    // pass A.  The buffer is refilled only after the copy engine has read it.
+    template <int N, bool RF, bool RESID, bool TS>
+    __device__ __forceinline__ void run_blocks(unsigned char *smem, int r, int j, const void *tmap) const {
         static_assert(RF, "rows-fastest launch");
         using SN = S<N>;
         constexpr int E = SN::E, ROWS = SN::ROWS;
@@ -1092,7 +1106,10 @@ struct GsRowMidT : PassBase {
         for (int rb = blockIdx.x; rb < nblocks; rb += gridDim.x, ++it) {
             const int buf = it & 1;
             __syncthreads();   // every thread is done with the other buffer
-            if (threadIdx.x == 0 && rb + (int)gridDim.x < nblocks) issue(rb + gridDim.x, buf ^ 1);
+            if (threadIdx.x == 0 && rb + (int)gridDim.x < nblocks) {
+                if constexpr (TS) bulk_wait_read_all();   // the other buffer's staged outputs have left
+                issue(rb + gridDim.x, buf ^ 1);
+            }
             mbar_wait(bars + buf, (parity >> buf) & 1u, err);
             parity ^= 1u << buf;
             unsigned char *base = smem + buf * BUF;
@@ -1116,10 +1133,32 @@ struct GsRowMidT : PassBase {
                                     }
                                     mid[(x - j) / SN::P] = amplitude_replace(v, s);
                                 });
-            fft_row<N, E, false>(xr, j, tw, [&](int, int x) -> float2 { return mid[(x - j) / SN::P]; },
-                                 [&](int, int kx, float2 v) {
-                                     if (valid) dst[(size_t)kx * nrows + y] = v;
-                                 });
+            if constexpr (TS) {
+                float2 *stg = reinterpret_cast<float2 *>(base);   // [kx][ROWS], over the field rows
+                fft_row_sync<N, E, false, false, true>(
+                    xr, j, tw, [&](int, int x) -> float2 { return mid[(x - j) / SN::P]; },
+                    [&](int, int kx, float2 v) { stg[kx * ROWS + r] = v; }, CtaSync{});
+                fence_proxy_async_smem();   // the staging writes, before the copy engine reads them
+                if (threadIdx.x < 32) {
+                    named_bar_sync(1, SN::THREADS);
+                    if (threadIdx.x == 0) {
+#pragma unroll 1
+                        for (int q = 0; q < N / kGsBox; ++q)
+                            tma_store_2d(tmap, stg + (size_t)q * kGsBox * ROWS, rb * ROWS, q * kGsBox);
+                        bulk_commit();
+                    }
+                } else {
+                    named_bar_arrive(1, SN::THREADS);
+                }
+            } else {
+                fft_row<N, E, false>(xr, j, tw, [&](int, int x) -> float2 { return mid[(x - j) / SN::P]; },
+                                     [&](int, int kx, float2 v) {
+                                         if (valid) dst[(size_t)kx * nrows + y] = v;
+                                     });
+            }
+        }
+        if constexpr (TS) {
+            if (threadIdx.x == 0) bulk_wait_all();   // the stores are complete before the grid is
         }
         if (RESID) {
 #pragma unroll
@@ -1141,7 +1180,15 @@ struct GsRowMidT : PassBase {
 struct GsRowMidTResid : GsRowMidT {
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
-        run_blocks<N, RF, true>(smem, r, j);
+        run_blocks<N, RF, true, false>(smem, r, j, nullptr);
+    }
+};
+// The two forms with the tensor-map store (launched with the map of dst).
+template <bool RESID>
+struct GsRowMidTS : GsRowMidT {
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j, const void *tmap) const {
+        run_blocks<N, RF, RESID, true>(smem, r, j, tmap);
     }
 };
 
@@ -1180,6 +1227,14 @@ struct GsColT : PassBase {
 
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
+        run_impl<N, RF, false>(smem, r, j, nullptr);
+    }
+
+    // TS: the transposed store through a tensor map, as in GsRowMidT (the
+    // inverse transform's outputs staged as [y][kx mod ROWS] over the block's
+    // field rows, boxes of ROWS kx x 256 y).
+    template <int N, bool RF, bool TS>
+    __device__ __forceinline__ void run_impl(unsigned char *smem, int r, int j, const void *tmap) const {
         static_assert(RF, "rows-fastest launch");
         using SN = S<N>;
         constexpr int E = SN::E, ROWS = SN::ROWS;
@@ -1230,7 +1285,10 @@ struct GsColT : PassBase {
             const int buf = it & 1;
             const int next = rb + gridDim.x;
             __syncthreads();   // every thread is done with the other field buffer
-            if (threadIdx.x == 0 && next < nblocks) issue_field(next, buf ^ 1);
+            if (threadIdx.x == 0 && next < nblocks) {
+                if constexpr (TS) bulk_wait_read_all();   // the other buffer's staged outputs have left
+                issue_field(next, buf ^ 1);
+            }
             if (!HT_EARLY && threadIdx.x == 0 && it > 0) issue_ht(rb);
             mbar_wait(bars + buf, (parity >> buf) & 1u, err);
             parity ^= 1u << buf;
@@ -1255,15 +1313,44 @@ struct GsColT : PassBase {
                     // the transfer rows, so the next block's may come in
                     if (nsync++ == 0 && HT_EARLY && threadIdx.x == 0 && next < nblocks) issue_ht(next);
                 };
-                fft_row_sync<N, E, true>(xr, j, twv, [&](int, int ky) -> float2 { return mid[(ky - j) / SN::P]; },
-                                         [&](int, int y, float2 v) {
-                                             if (valid) dst[(size_t)y * nx + kx] = v;
-                                         },
-                                         sync);
+                if constexpr (TS) {
+                    float2 *stg = reinterpret_cast<float2 *>(smem + buf * FB);   // [y][ROWS], over the field rows
+                    fft_row_sync<N, E, true, false, true>(
+                        xr, j, twv, [&](int, int ky) -> float2 { return mid[(ky - j) / SN::P]; },
+                        [&](int, int y, float2 v) { stg[y * ROWS + r] = v; }, sync);
+                    fence_proxy_async_smem();   // the staging writes, before the copy engine reads them
+                    if (threadIdx.x < 32) {
+                        named_bar_sync(1, SN::THREADS);
+                        if (threadIdx.x == 0) {
+#pragma unroll 1
+                            for (int q = 0; q < N / kGsBox; ++q)
+                                tma_store_2d(tmap, stg + (size_t)q * kGsBox * ROWS, rb * ROWS, q * kGsBox);
+                            bulk_commit();
+                        }
+                    } else {
+                        named_bar_arrive(1, SN::THREADS);
+                    }
+                } else {
+                    fft_row_sync<N, E, true>(xr, j, twv,
+                                             [&](int, int ky) -> float2 { return mid[(ky - j) / SN::P]; },
+                                             [&](int, int y, float2 v) {
+                                                 if (valid) dst[(size_t)y * nx + kx] = v;
+                                             },
+                                             sync);
+                }
             };
             if constexpr (TWS) go(tws);
             else go(opaque(this->tw));   // twiddles are re-read per block, not held in registers
         }
+        if constexpr (TS) {
+            if (threadIdx.x == 0) bulk_wait_all();   // the stores are complete before the grid is
+        }
+    }
+};
+struct GsColTS : GsColT {
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j, const void *tmap) const {
+        run_impl<N, RF, true>(smem, r, j, tmap);
     }
 };
 

@@ -158,6 +158,12 @@ __device__ __forceinline__ void tma_store_3d(const void *tmap, const void *src, 
                  "r"(smem_addr(src)), "r"(x), "r"(y), "r"(z)
                  : "memory");
 }
+// The 2-D form: element coordinates (x, y).
+__device__ __forceinline__ void tma_store_2d(const void *tmap, const void *src, int x, int y) {
+    asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(tmap),
+                 "r"(smem_addr(src)), "r"(x), "r"(y)
+                 : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 // The issuing thread's committed bulk stores have read their shared-memory source.
 __device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
