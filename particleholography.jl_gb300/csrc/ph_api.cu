@@ -926,13 +926,13 @@ EncodeTiledFn encode_tiled() {
 }
 
 // Tensor map of the slice intermediate T = [nb][ny_out][nx] float2 (8-byte
-// elements) for pass A's tiled store: boxes of 4 kx x 256 y x 1 slice.
-bool t_store_map(CUtensorMap *tm, float2 *t, int nx, int ny_out, int nb) {
+// elements) for pass A's tiled store: boxes of box_kx kx x 256 y x 1 slice.
+bool t_store_map(CUtensorMap *tm, float2 *t, int nx, int ny_out, int nb, int box_kx) {
     const EncodeTiledFn enc = encode_tiled();
-    if (enc == nullptr || ((uintptr_t)t & 15) != 0 || nx % 4 != 0) return false;
+    if (enc == nullptr || ((uintptr_t)t & 15) != 0 || nx % 4 != 0 || box_kx < 4 || box_kx > 32) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny_out, (cuuint64_t)nb};
     const cuuint64_t strides[2] = {(cuuint64_t)nx * 8, (cuuint64_t)nx * ny_out * 8};
-    const cuuint32_t box[3] = {4, (cuuint32_t)ReconATStore::kBoxY, 1};
+    const cuuint32_t box[3] = {(cuuint32_t)box_kx, (cuuint32_t)ReconATStore::kBoxY, 1};
     const cuuint32_t estr[3] = {1, 1, 1};
     return enc(tm, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, t, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
@@ -979,7 +979,7 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
             a.err = static_cast<int *>(ctx->small);
         };
         CUtensorMap tm;
-        if (recon_a_tstore(ny) && y0 == 0 && ny_out == ny && t_store_map(&tm, t, nx, ny_out, nb)) {
+        if (recon_a_tstore(ny) && y0 == 0 && ny_out == ny && t_store_map(&tm, t, nx, ny_out, nb, recon_a_tstore_box(ny))) {
             ReconATStore a{};
             fill_a(a);
             PH_TRY(pass(ctx, s, "recon_a", [&] { return launch_recon_a_tstore(ny, a, tm, nb, s); }));

@@ -210,6 +210,7 @@ cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s);
 // Pass A with the tensor-map transposed store (lengths where recon_a_tstore holds;
 // tm: T as [nbatch][ny_out = n][nx] 8-byte elements, boxes of 4 x 256 x 1).
 bool recon_a_tstore(int n);
+int recon_a_tstore_box(int n);   // kx per box (rows per CTA x CTAs per cluster)
 cudaError_t launch_recon_a_tstore(int n, const ReconATStore &b, const CUtensorMap &tm, int nbatch, cudaStream_t s);
 cudaError_t launch_recon_a_group(int n, const ReconAGrouped &b, cudaStream_t s);
 // The persistent GS passes with the tensor-map store (lengths where

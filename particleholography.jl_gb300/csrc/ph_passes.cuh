@@ -437,7 +437,8 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
     // as [y][kx mod 4] (over the exchange rows, after a barrier) and one
     // thread stores the boxes: the LSU no longer carries 8 sectors of 8
     // different lines per warp store.
-    //  - 4 rows per CTA: the CTA stages and stores all y.
+    //  - 4 rows or more per CTA (lengths 256 .. 2048: 8192 / N rows, boxes of
+    //    that many kx): the CTA stages and stores all y.
     //  - 2 rows per CTA, clusters of 2: CTA c stages y in [c N/2, (c+1) N/2)
     //    of all 4 rows; each CTA writes its outputs into the owner's staging
     //    (distributed shared memory for the peer's half) between two cluster
@@ -448,7 +449,7 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
     template <int N>
     static constexpr bool tstore_ok() {
         constexpr int R = Shape<N, EPT, TT>::ROWS;
-        return N >= 2 * kBoxY && ((R == 4 && cluster<N>() == 1) || (R == 2 && cluster<N>() == 2));
+        return N % kBoxY == 0 && ((R >= 4 && R <= 32 && cluster<N>() == 1) || (R == 2 && cluster<N>() == 2 && (N / 2) % kBoxY == 0));
     }
 
     template <int N, bool RF>
@@ -456,7 +457,7 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
         using S = Shape<N, EPT, TT>;
         constexpr int ROWS = S::ROWS;
         constexpr int FORM = form<N, RF>();
-        static_assert(!TSTORE || tstore_ok<N>(), "tensor-map store: 4 rows per CTA or 2 in a cluster of 2, N >= 512");
+        static_assert(!TSTORE || tstore_ok<N>(), "tensor-map store: 4..32 rows per CTA or 2 in a cluster of 2, N a multiple of 256");
         unsigned char *xbase = smem + stage_total<N, RF>();
         constexpr int CS = cluster<N>();
         // The CTAs of one row block (its `gridDim.y` slice groups) are consecutive
