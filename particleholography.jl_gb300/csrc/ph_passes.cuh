@@ -559,11 +559,15 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
                 // First barrier: the previous slice's boxes have left the
                 // staging.  Last: both CTAs have read their last stage's
                 // inputs, so the staging (the peer's included) may be written.
+                // Its arrival is relaxed: the butterfly has consumed every
+                // value read, so the reads are complete (a release arrival
+                // made `membar` the third stall of the capture).
                 const auto sync = [&nsync]() {
                     const int i = nsync++;
                     if (i == 0 && threadIdx.x == 0) bulk_wait_read_all();
                     if (i == LAST_SYNC) {
-                        cluster_sync();
+                        cluster_arrive_relaxed();
+                        cluster_wait();
                     } else {
                         __syncthreads();
                     }
