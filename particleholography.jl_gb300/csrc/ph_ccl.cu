@@ -139,6 +139,23 @@ __global__ void __launch_bounds__(kCclBlockX * kCclBlockY)
         sv[ly][lx] = (y < rows && x < cols) ? img[y * cols + x] : T(0);   // outside: background
     }
     __syncthreads();
+    // A tile of one foreground value, inside the image and one slice, is one
+    // component whose root is its first pixel: label it without hooking (in a
+    // projection thresholded into near-total foreground every tile is one,
+    // and the shared-memory hooks of its 1024 pixels all meet at one root).
+    {
+        const T v0 = sv[0][0];
+        bool same = ccl_fg<T>(v0) && ty0 + kTile <= rows && tx0 + kTile <= cols &&
+                    (ty0 % slice_rows) + kTile <= slice_rows;
+#pragma unroll
+        for (int k = 0; k < K; ++k) same = same && ccl_eq(sv[threadIdx.y + k * kCclBlockY][lx], v0);
+        if (__syncthreads_and(same)) {
+            const uint32_t root = (uint32_t)(ty0 * cols + tx0);
+#pragma unroll
+            for (int k = 0; k < K; ++k) lab[(ty0 + threadIdx.y + k * kCclBlockY) * cols + tx0 + lx] = root;
+            return;
+        }
+    }
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const int ly = threadIdx.y + k * kCclBlockY;

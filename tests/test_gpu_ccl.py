@@ -62,6 +62,35 @@ def test_rectangular_grids(ph, cuda, shape):
     assert np.array_equal(_labels(ph, img, cuda, reference_grid=False), want_2d)
 
 
+@pytest.mark.parametrize("case", ["near_full", "blocks_48", "partial_tiles"])
+def test_uniform_tiles_bit_exact(ph, cuda, case):
+    """Tiles of one foreground value take the tile-local fast path (one root,
+    no hooks): near-total foreground (a projection thresholded high), blocks of
+    three values 48 pixels wide (uniform tiles beside mixed ones), and a
+    1000^2 image whose edge tiles are partial."""
+    rng = np.random.default_rng(len(case))
+    if case == "blocks_48":
+        img = np.kron(rng.integers(0, 3, (11, 11)), np.ones((48, 48)))[:512, :512].astype(np.float32)
+    else:
+        n = 1024 if case == "near_full" else 1000
+        img = np.ones((n, n), np.float32)
+        img.flat[rng.integers(0, n * n, 60)] = 0.0
+    lab = _labels(ph, img, cuda)
+    assert np.array_equal(lab, occl.connected_component_labeling(img))
+
+
+def test_uniform_tiles_across_slices(ph, cuda):
+    """Batched slices 48 rows high: a tile of one value that straddles a slice
+    boundary is two components, one per slice."""
+    rng = np.random.default_rng(11)
+    vol = np.ones((3, 48, 96), np.float32)
+    vol[1, 20, 40] = 0.0
+    vol[2] = (rng.random((48, 96)) < 0.9).astype(np.float32)
+    lab = to_np(ph.cu_connected_component_labeling_batch(to_dev(vol, cuda))).astype(np.uint32)
+    for k in range(3):
+        assert np.array_equal(lab[k], occl.connected_component_labeling(vol[k]))
+
+
 def test_snake_long_chains(ph, cuda):
     """A single serpentine component exercises long union chains."""
     n = 512
