@@ -118,12 +118,14 @@ __device__ __forceinline__ float2 twiddle_fp64(int i, int n) {   // W_n^i rounde
     return make_float2((float)c, (float)s);
 }
 
-__global__ void k_phase_table(double2 *tab, int n) {
+// w_j = (cos, sin)(2 pi j / n) in FP64, stored as FP32 pairs (cos hi, cos lo, sin hi, sin lo).
+__global__ void k_phase_table(float4 *tab, int n) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     double s, c;
     sincospi(2.0 * (double)j / (double)n, &s, &c);
-    tab[j] = make_double2(c, s);
+    const float ch = (float)c, sh = (float)s;
+    tab[j] = make_float4(ch, (float)(c - (double)ch), sh, (float)(s - (double)sh));
 }
 
 __global__ void k_twiddle(float2 *tw, int n) {
@@ -1302,7 +1304,7 @@ int32_t ph_create(int32_t device, size_t hbm_budget_bytes, ph_ctx **out) {
     if (cudaEventCreateWithFlags(&ctx->done, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->capture_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&ctx->small, 256) != cudaSuccess || cudaMemset(ctx->small, 0, 256) != cudaSuccess ||
-        cudaMalloc(&ctx->phase_tab, sizeof(double2) * kPhaseTable) != cudaSuccess) {
+        cudaMalloc(&ctx->phase_tab, sizeof(float4) * kPhaseTable) != cudaSuccess) {
         cudaGetLastError();
         ph_destroy(ctx);
         return PH_ERR_CUDA;

@@ -51,7 +51,7 @@ struct ph_ctx {
     size_t scratch_bytes = 0;
 
     // unit vectors (cos, sin)(2 pi j / 4096) in FP64 for the spectrum's phase rates
-    double2 *phase_tab = nullptr;
+    float4 *phase_tab = nullptr;
 
     // small fixed device area: [0] loop-limit error flag (int), [8..) 4 doubles of accumulators
     void *small = nullptr;

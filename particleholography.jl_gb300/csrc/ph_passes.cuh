@@ -252,31 +252,46 @@ struct FwdRowsT : PassBase {
 
 // ---------------------------------------------------------------- spectrum state
 
-// Phase of h as a 32-bit fixed-point fraction of a turn, to ~1e-10 rad with
-// FP64 only where FP32 would lose it: the nearest of 4096 table angles j / 4096
-// turns (FP32 atan2 picks it), the rotation h * conj(w_j) in FP64 (tab holds
-// w_j = (cos, sin)(2 pi j / 4096), FP64), and the remaining angle |phi| <~
-// pi / 4096 by FP32 atan2, whose ~2 ulp relative error is then ~2e-10 rad.
-// (FP64 atan2 throughout costs ~7x more FP64 operations, which GB300 runs at
-// 1/64 of its FP32 rate.)
+// Phase of h as a 32-bit fixed-point fraction of a turn, to ~1e-10 rad: the
+// nearest of 4096 table angles j / 4096 turns (FP32 atan2 picks it), the
+// rotation z = h * conj(w_j), and the remaining angle |phi| <~ pi / 4096 by
+// FP32 atan2, whose ~2 ulp relative error is then ~2e-10 rad.  tab holds w_j =
+// (cos, sin)(2 pi j / 4096), each as an FP32 pair hi + lo (computed in FP64).
+// z's real part is ~|h| and needs FP32 only; its imaginary part hy wx - hx wy
+// cancels to ~|h| pi / 4096, so it is formed from error-free products (fma)
+// of the hi words, an error-free difference, and the lo words' products: FP32
+// arithmetic to the accuracy the FP64 form had, which GB300 runs at 1/64 of
+// its FP32 rate (the FP64 form spent about half of the spectrum pass there).
 constexpr int kPhaseTable = 4096;
-__device__ __forceinline__ uint32_t phase_turns_u32(float2 h, const double2 *__restrict__ tab) {
+__device__ __forceinline__ uint32_t phase_turns_u32(float2 h, const float4 *__restrict__ tab) {
     const float a0 = atan2f(h.y, h.x);
     const int i = __float2int_rn(a0 * ((float)kPhaseTable / 6.28318530717958647692f));
-    const double2 w = __ldg(tab + (i & (kPhaseTable - 1)));
-    const double zx = (double)h.x * w.x + (double)h.y * w.y;   // h * conj(w)
-    const double zy = (double)h.y * w.x - (double)h.x * w.y;
-    const float phi = atan2f((float)zy, (float)zx);
+    const float4 w = __ldg(tab + (i & (kPhaseTable - 1)));   // (cos hi, cos lo, sin hi, sin lo)
+    const float zx = __fmaf_rn(h.x, w.x, __fmul_rn(h.y, w.z));
+    const float p1 = __fmul_rn(h.y, w.x), e1 = __fmaf_rn(h.y, w.x, -p1);   // hy wx_hi = p1 + e1 exactly
+    const float p2 = __fmul_rn(h.x, w.z), e2 = __fmaf_rn(h.x, w.z, -p2);   // hx wy_hi = p2 + e2 exactly
+    const float d = __fsub_rn(p1, p2);                                       // p1 - p2 = d + ed exactly
+    const float bv = __fsub_rn(d, p1);
+    const float ed = __fadd_rn(__fsub_rn(p1, __fsub_rn(d, bv)), __fsub_rn(-p2, bv));
+    const float lo = __fmaf_rn(h.y, w.y, -__fmul_rn(h.x, w.w));             // the lo words
+    const float zy = __fadd_rn(d, __fadd_rn(__fadd_rn(ed, __fsub_rn(e1, e2)), lo));
+    const float phi = atan2f(zy, zx);
     return ((uint32_t)i << 20) + (uint32_t)__float2int_rn(phi * (4294967296.0f / 6.28318530717958647692f));
 }
 
-// log2 |h|.  |h| - 1 comes from (|h|^2 - 1) in FP64 from exact products (no
-// cancellation error near |h| = 1) over |h| + 1 in FP32, then log1pf.  h = 0
-// gives -1e30 rather than -inf, so that k log2|h| is 0 at k = 0 (|h|^0 = 1)
-// and |h|^k underflows to 0 for every k >= 1.
+// log2 |h|.  |h|^2 - 1 from error-free products (fma) and an error-free sum
+// of them (s - 1 is exact for s in [1/2, 2]), so that there is no cancellation
+// error near |h| = 1, over |h| + 1, then log1pf.  h = 0 gives -1e30 rather
+// than -inf, so that k log2|h| is 0 at k = 0 (|h|^0 = 1) and |h|^k underflows
+// to 0 for every k >= 1.
 __device__ __forceinline__ float log2_modulus(float2 h) {
-    const double v = (double)h.x * h.x + (double)h.y * h.y - 1.0;
-    const float w = (float)v / (sqrtf(fmaf(h.x, h.x, h.y * h.y)) + 1.0f);
+    const float a = __fmul_rn(h.x, h.x), ea = __fmaf_rn(h.x, h.x, -a);
+    const float b = __fmul_rn(h.y, h.y), eb = __fmaf_rn(h.y, h.y, -b);
+    const float s = __fadd_rn(a, b);
+    const float bv = __fsub_rn(s, a);
+    const float es = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bv)), __fsub_rn(b, bv));
+    const float v = __fadd_rn(__fsub_rn(s, 1.0f), __fadd_rn(es, __fadd_rn(ea, eb)));
+    const float w = v / (sqrtf(fmaf(h.x, h.x, h.y * h.y)) + 1.0f);
     return fmaxf(log1pf(w) * 1.44269504088896340736f, -1e30f);
 }
 
@@ -287,7 +302,7 @@ struct SpectrumCols : PassBase {
     const float2 *a1;        // [nx][ny]
     const float2 *hf, *hdz;  // centred [ny][nx]
     const float *lpf;        // centred [ny][nx] low-pass filter, or null
-    const double2 *ptab;     // kPhaseTable unit vectors (phase_turns_u32)
+    const float4 *ptab;      // kPhaseTable unit vectors as FP32 pairs (phase_turns_u32)
     float4 *state;           // [nx][ny]
     const float2 *tw;
     int nx, ny;
