@@ -955,6 +955,23 @@ bool gs_store_map(CUtensorMap *tm, float2 *p, int inner, int outer, int rows) {
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Tensor map of the T slots of a grouped launch: item i's T = [nb][ny][nx]
+// float2 at t + i * item_bytes; boxes of box_kx kx x 256 y x 1 slice x 1 item.
+bool t_store_map_items(CUtensorMap *tm, float2 *t, int nx, int ny, int nb, int nitems, size_t item_bytes,
+                       int box_kx) {
+    const EncodeTiledFn enc = encode_tiled();
+    if (enc == nullptr || ((uintptr_t)t & 15) != 0 || nx % 4 != 0 || box_kx < 4 || box_kx > 32 ||
+        item_bytes % 16 != 0)
+        return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nb, (cuuint64_t)nitems};
+    const cuuint64_t strides[3] = {(cuuint64_t)nx * 8, (cuuint64_t)nx * ny * 8, (cuuint64_t)item_bytes};
+    const cuuint32_t box[4] = {(cuuint32_t)box_kx, (cuuint32_t)ReconATStore::kBoxY, 1, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    return enc(tm, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, t, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // The slice loop of a reconstruction: pass A and pass B per batch, then the
 // projection unpacking.
 int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin, void *vol, int vol_dtype, int nx,
@@ -1231,7 +1248,25 @@ int issue_recon_group(ph_ctx *ctx, const std::vector<const ph_recon_item *> &its
         a.group = a.item_group(0);
         a.nitems = G;
         a.err = static_cast<int *>(ctx->small);
-        PH_TRY(pass(ctx, s, "recon_a", [&] { return launch_recon_a_group(ny, a, s); }));
+        CUtensorMap tm;
+        if (recon_a_group_tstore(ny) &&
+            t_store_map_items(&tm, a.t, nx, ny, L.batch, G, ib, recon_a_tstore_box(ny))) {
+            ReconAGroupedTStore at{};
+            static_cast<ReconItems &>(at) = static_cast<const ReconItems &>(a);
+            at.state = a.state;
+            at.t = a.t;
+            at.tw = a.tw;
+            at.err = a.err;
+            at.nx = a.nx;
+            at.ny_out = a.ny_out;
+            at.y0 = a.y0;
+            at.k0 = a.k0;
+            at.nbatch = a.nbatch;
+            at.group = a.group;
+            PH_TRY(pass(ctx, s, "recon_a", [&] { return launch_recon_a_group_tstore(ny, at, tm, s); }));
+        } else {
+            PH_TRY(pass(ctx, s, "recon_a", [&] { return launch_recon_a_group(ny, a, s); }));
+        }
         b.t = reinterpret_cast<const float2 *>(slot(0, L.t));
         b.tw = tw_x;
         b.proj64 = reinterpret_cast<unsigned long long *>(slot(0, L.p64));

@@ -107,7 +107,8 @@ cudaError_t launch_one(const Body &body, int nrows, int grid_y, cudaStream_t s, 
 // Body::cluster<N>() CTAs, persistent grids and programmatic dependents as in
 // launch_one).
 template <int N, bool ROW_FAST, class Body>
-cudaError_t launch_one_tm(const Body &body, const CUtensorMap &tm, int nrows, int grid_y, cudaStream_t s) {
+cudaError_t launch_one_tm(const Body &body, const CUtensorMap &tm, int nrows, int grid_y, cudaStream_t s,
+                          int grid_z = 1) {
     auto kern = k_pass_tm<N, ROW_FAST, Body>;
     constexpr size_t smem = Body::template smem<N, ROW_FAST>();
     static_assert(smem <= kSmemMax, "pass needs more shared memory than a CTA has");
@@ -144,7 +145,7 @@ cudaError_t launch_one_tm(const Body &body, const CUtensorMap &tm, int nrows, in
     constexpr int CS = Body::template cluster<N>();
     static_assert(CS == 1 || !Body::template pdl<N>(), "cluster or programmatic-dependent launch, not both");
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((gx + CS - 1) / CS * CS, grid_y, 1);
+    cfg.gridDim = dim3((gx + CS - 1) / CS * CS, grid_y, grid_z);
     cfg.blockDim = dim3(S::THREADS);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
@@ -213,6 +214,11 @@ bool recon_a_tstore(int n);
 int recon_a_tstore_box(int n);   // kx per box (rows per CTA x CTAs per cluster)
 cudaError_t launch_recon_a_tstore(int n, const ReconATStore &b, const CUtensorMap &tm, int nbatch, cudaStream_t s);
 cudaError_t launch_recon_a_group(int n, const ReconAGrouped &b, cudaStream_t s);
+// The grouped form with the tensor-map store, at the lengths where
+// recon_a_tstore holds with one CTA per box (256 .. 2048); tm: the items' T
+// slots as (kx, y, slice, item), boxes of recon_a_tstore_box(n) kx x 256 y.
+bool recon_a_group_tstore(int n);
+cudaError_t launch_recon_a_group_tstore(int n, const ReconAGroupedTStore &b, const CUtensorMap &tm, cudaStream_t s);
 // The persistent GS passes with the tensor-map store (lengths where
 // gs_tstore_len holds; tm: dst as a 2-D tensor of 8-byte elements, inner
 // dimension the rows' index, boxes of rows-per-block x 256).

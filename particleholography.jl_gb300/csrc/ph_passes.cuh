@@ -624,8 +624,14 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
                     named_bar_sync(1, S::THREADS);
                     if (threadIdx.x == 0) {
 #pragma unroll 1
-                        for (int q = 0; q < N / kBoxY; ++q)
-                            tma_store_3d(tmap, stg + (size_t)q * kBoxY * ROWS, kx0, q * kBoxY, b);
+                        for (int q = 0; q < N / kBoxY; ++q) {
+                            if constexpr (GROUPED) {   // one map over the items' slots: (kx, y, slice, item)
+                                tma_store_4d(tmap, stg + (size_t)q * kBoxY * ROWS, kx0, q * kBoxY, b,
+                                             (int)blockIdx.z);
+                            } else {
+                                tma_store_3d(tmap, stg + (size_t)q * kBoxY * ROWS, kx0, q * kBoxY, b);
+                            }
+                        }
                         bulk_commit();
                     }
                 } else {
@@ -684,6 +690,7 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
 using ReconA = ReconAT<false>;
 using ReconATStore = ReconAT<false, true>;
 using ReconAGrouped = ReconAT<true>;
+using ReconAGroupedTStore = ReconAT<true, true>;
 
 // ---------------------------------------------------------------- reconstruction pass B
 

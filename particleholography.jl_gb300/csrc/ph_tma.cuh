@@ -158,6 +158,12 @@ __device__ __forceinline__ void tma_store_3d(const void *tmap, const void *src, 
                  "r"(smem_addr(src)), "r"(x), "r"(y), "r"(z)
                  : "memory");
 }
+// The 4-D form: element coordinates (x, y, z, w).
+__device__ __forceinline__ void tma_store_4d(const void *tmap, const void *src, int x, int y, int z, int w) {
+    asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(tmap),
+                 "r"(smem_addr(src)), "r"(x), "r"(y), "r"(z), "r"(w)
+                 : "memory");
+}
 // The 2-D form: element coordinates (x, y).
 __device__ __forceinline__ void tma_store_2d(const void *tmap, const void *src, int x, int y) {
     asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(tmap),
