@@ -201,29 +201,43 @@ __global__ void __launch_bounds__(kCclBlockX * kCclBlockY)
 // ---- merge across tile borders: the pairs whose earlier neighbour lies in
 // another tile (W, NW of the left column; NW, N, NE of the top row; NE of the
 // right column) are hooked in the global parents.  Grid: (row tiles, column
-// tiles), 128 threads, 94 border pixels per tile.
+// tiles), 128 threads, 94 border pixels per tile.  Within a warp, pairs whose
+// current parents are the same two nodes link the same two trees, so one lane
+// of each such set hooks (between tiles of one value, as in a near-total
+// foreground, one hook per neighbour tile instead of one per border pixel).
+__device__ __forceinline__ void ccl_hook_dedup(uint32_t *lab, bool cond, uint32_t a, uint32_t b, int64_t limit,
+                                               int *err) {
+    const unsigned act = __ballot_sync(0xffffffffu, cond);
+    if (cond) {
+        const unsigned long long key = ((unsigned long long)__ldcg(lab + a) << 32) | __ldcg(lab + b);
+        const unsigned peers = __match_any_sync(act, key);
+        if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) ccl_hook(lab, a, b, limit, err);
+    }
+}
+
 template <class T>
 __global__ void k_ccl_border(const T *__restrict__ img, uint32_t *lab, int64_t rows, int64_t cols, int64_t slice_rows,
                              int64_t limit, int *err) {
     const int t = threadIdx.x;
-    int ly, lx;
+    int ly = 0, lx = 0;
+    bool on = true;   // every thread takes part in the warp votes below
     if (t < kTile) { ly = 0; lx = t; }
     else if (t < 2 * kTile - 1) { ly = t - (kTile - 1); lx = 0; }
     else if (t < 3 * kTile - 2) { ly = t - (2 * kTile - 2); lx = kTile - 1; }
-    else return;
+    else on = false;
     const int64_t y = (int64_t)blockIdx.x * kTile + ly, x = (int64_t)blockIdx.y * kTile + lx;
-    if (y >= rows || x >= cols) return;
-    const int64_t i = y * cols + x;
-    const T v = img[i];
-    if (!ccl_fg<T>(v)) return;
-    if (lx == 0 && x > 0 && ccl_eq(img[i - 1], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)(i - 1), limit, err);
-    if (y % slice_rows != 0) {
-        const int64_t u = i - cols;
-        if ((lx == 0 || ly == 0) && x > 0 && ccl_eq(img[u - 1], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)(u - 1), limit, err);
-        if (ly == 0 && ccl_eq(img[u], v)) ccl_hook(lab, (uint32_t)i, (uint32_t)u, limit, err);
-        if ((ly == 0 || lx == kTile - 1) && x + 1 < cols && ccl_eq(img[u + 1], v))
-            ccl_hook(lab, (uint32_t)i, (uint32_t)(u + 1), limit, err);
-    }
+    on = on && y < rows && x < cols;
+    const int64_t i = on ? y * cols + x : 0;
+    const T v = on ? img[i] : T(0);
+    on = on && ccl_fg<T>(v);
+    const bool up = on && y % slice_rows != 0;
+    const int64_t u = i - cols;
+    ccl_hook_dedup(lab, on && lx == 0 && x > 0 && ccl_eq(img[i - 1], v), (uint32_t)i, (uint32_t)(i - 1), limit, err);
+    ccl_hook_dedup(lab, up && (lx == 0 || ly == 0) && x > 0 && ccl_eq(img[u - 1], v), (uint32_t)i, (uint32_t)(u - 1),
+                   limit, err);
+    ccl_hook_dedup(lab, up && ly == 0 && ccl_eq(img[u], v), (uint32_t)i, (uint32_t)u, limit, err);
+    ccl_hook_dedup(lab, up && (ly == 0 || lx == kTile - 1) && x + 1 < cols && ccl_eq(img[u + 1], v), (uint32_t)i,
+                   (uint32_t)(u + 1), limit, err);
 }
 
 template <class T>
