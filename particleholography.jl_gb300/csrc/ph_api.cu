@@ -1605,9 +1605,9 @@ int32_t ph_phase_retrieval(ph_ctx *ctx, void *out, const float *holo1, const flo
             r1.src = bufb; r1.holo = amp1; r1.dst = bufa; r1.tw = tw_x; r1.err = err; r1.nrows = ny;
             PH_TRY(pass(ctx, s, "gs_row_mid",[&] { return row(r1); }));
         } else {
-            GsRow<ROW_FINAL> r1{};
-            r1.src = bufb; r1.holo = holo1; r1.dst = o; r1.tw = tw_x; r1.nrows = ny;
-            PH_TRY(pass(ctx, s, "gs_row_final",[&] { return launch_gs_row(nx, r1, s); }));
+            GsRowMidT r1{};   // the persistent pass in its final form: natural store into the output
+            r1.src = bufb; r1.holo = amp1; r1.dst = o; r1.tw = tw_x; r1.err = err; r1.nrows = ny;
+            PH_TRY(pass(ctx, s, "gs_row_final",[&] { return launch_gs_row_final_t(nx, r1, s); }));
         }
     }
     for (int it = 0; it < priter && !staged; ++it) {

@@ -22,6 +22,12 @@ cudaError_t launch_gs_row_t(int n, const GsRowMidT &b, cudaStream_t s) {
 
 bool gs_row_staged(int n) { return staged_len<GsRowMidT>(n); }
 
+cudaError_t launch_gs_row_final_t(int n, const GsRowMidT &b, cudaStream_t s) {
+    GsRowFinalT f{};
+    static_cast<GsRowMidT &>(f) = b;
+    return launch_staged_len<true>(n, f, b.nrows, s);
+}
+
 template <bool RESID>
 cudaError_t launch_gs_row_ts_form(int n, const GsRowMidT &b, const CUtensorMap &tm, cudaStream_t s) {
     GsRowMidTS<RESID> ts{};

@@ -241,6 +241,8 @@ cudaError_t launch_gs_col(int n, const GsCol &b, cudaStream_t s);
 bool gs_row_staged(int n);
 bool gs_col_staged(int n);
 cudaError_t launch_gs_row_t(int n, const GsRowMidT &b, cudaStream_t s);
+// The last plane-1 pass (dst = [ny][nx], natural order), persistent.
+cudaError_t launch_gs_row_final_t(int n, const GsRowMidT &b, cudaStream_t s);
 cudaError_t launch_gs_col_t(int n, const GsColT &b, cudaStream_t s);
 // Split-precision tensor-core pass B (ph_pass_tc.cuh) for the projection.
 struct ReconBTc;

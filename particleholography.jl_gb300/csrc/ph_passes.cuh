@@ -1096,7 +1096,9 @@ struct GsRowMidT : PassBase {
     // staged as [kx][y mod ROWS] over the block's field rows and one thread
     // stores them in boxes of ROWS y x 256 kx (whole 32-byte sectors), as in
     // pass A.  The buffer is refilled only after the copy engine has read it.
-    template <int N, bool RF, bool RESID, bool TS>
+    // FINAL: the last plane-1 pass of a call: the inverse transform and the
+    // amplitude replacement only, stored in natural order (dst = [ny][nx]).
+    template <int N, bool RF, bool RESID, bool TS, bool FINAL = false>
     __device__ __forceinline__ void run_blocks(unsigned char *smem, int r, int j, const void *tmap) const {
         static_assert(RF, "rows-fastest launch");
         using SN = S<N>;
@@ -1149,6 +1151,13 @@ struct GsRowMidT : PassBase {
             // j + s P (s < E), the very columns the forward transform's first
             // stage reads: the amplitude replacement passes between them in
             // registers.
+            if constexpr (FINAL) {
+                fft_row<N, E, true>(xr, j, tw, [&](int, int x) -> float2 { return xr[x]; },
+                                    [&](int, int x, float2 v) {
+                                        if (valid) dst[(size_t)y * N + x] = amplitude_replace(v, hr[x]);
+                                    });
+                continue;
+            }
             float2 mid[E];
             fft_row<N, E, true>(xr, j, tw, [&](int, int x) -> float2 { return xr[x]; },
                                 [&](int, int x, float2 v) {
@@ -1208,6 +1217,13 @@ struct GsRowMidTResid : GsRowMidT {
     template <int N, bool RF>
     __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
         run_blocks<N, RF, true, false>(smem, r, j, nullptr);
+    }
+};
+// The last plane-1 pass in the persistent form (natural store).
+struct GsRowFinalT : GsRowMidT {
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j) const {
+        run_blocks<N, RF, false, false, true>(smem, r, j, nullptr);
     }
 };
 // The two forms with the tensor-map store (launched with the map of dst).
