@@ -703,6 +703,38 @@ struct Spectrum {
     const float2 *tw_x, *tw_y;
 };
 
+// cuTensorMapEncodeTiled, looked up through the runtime's driver entry point
+// (the library does not link the driver library); null if unavailable.
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// Tensor map of a centred transfer [ny][nx] (8-byte elements) for the staged
+// spectrum pass: boxes of `rows` columns x 256 rows.
+bool tf_load_map(CUtensorMap *tm, const float2 *h, int nx, int ny, int rows) {
+    const EncodeTiledFn enc = encode_tiled();
+    if (enc == nullptr || ((uintptr_t)h & 15) != 0 || nx % 2 != 0 || rows < 2 || rows > 32) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)nx, (cuuint64_t)ny};
+    const cuuint64_t strides[1] = {(cuuint64_t)nx * 8};
+    const cuuint32_t box[2] = {(cuuint32_t)rows, 256};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(tm, CU_TENSOR_MAP_DATA_TYPE_UINT64, 2, const_cast<float2 *>(h), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // Forward FFT of the (optionally mean-padded) wavefront and the spectrum state.
 // nx, ny: transform size; a1: scratch [nx][ny] complex.  With `holo` (and wf
 // NULL) the wavefront is sqrt(holo) + 0i, formed in the first FFT stage.
@@ -751,6 +783,17 @@ int issue_spectrum(ph_ctx *ctx, const float2 *wf, const float2 *hf, const float2
     c.nx = nx;
     c.ny = ny;
     c.scale = (float)(1.0 / ((double)nx * (double)ny));
+    // the transfers staged by tensor-map boxes where the lengths allow it
+    const int rows = spectrum_staged_rows(ny);
+    CUtensorMap tm_hf, tm_hdz;
+    if (lpf == nullptr && rows > 0 && nx % (2 * rows) == 0 &&
+        tf_load_map(&tm_hf, hf, nx, ny, rows) && tf_load_map(&tm_hdz, hdz, nx, ny, rows)) {
+        SpectrumColsT ct{};
+        static_cast<SpectrumCols &>(ct) = c;
+        ct.err = static_cast<int *>(ctx->small);
+        PH_TRY(pass(ctx, s, "spectrum", [&] { return launch_spectrum_staged(ny, ct, tm_hf, tm_hdz, s); }));
+        return PH_OK;
+    }
     PH_TRY(pass(ctx, s, "spectrum", [&] { return launch_spectrum(ny, c, s); }));
     return PH_OK;
 }
@@ -907,24 +950,6 @@ int recon_group(int nbatch, int nx_rows_a, bool chain, int cap_override = 0) {
         if (g > 32 && ctas >= 16LL * sms) cap = 64;
     }
     return std::max(1, std::min(cap, nbatch / groups));
-}
-
-// cuTensorMapEncodeTiled, looked up through the runtime's driver entry point
-// (the library does not link the driver library); null if unavailable.
-using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiledFn encode_tiled() {
-    static const EncodeTiledFn fn = [] {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            q != cudaDriverEntryPointSuccess)
-            p = nullptr;
-        return reinterpret_cast<EncodeTiledFn>(p);
-    }();
-    return fn;
 }
 
 // Tensor map of the slice intermediate T = [nb][ny_out][nx] float2 (8-byte

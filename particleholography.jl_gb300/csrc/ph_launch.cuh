@@ -166,6 +166,31 @@ cudaError_t launch_one_tm(const Body &body, const CUtensorMap &tm, int nrows, in
     return cudaLaunchKernelEx(&cfg, kern, body, tm);
 }
 
+// A plain launch of k_pass_tm2 (two tensor maps), one grid row.
+template <int N, bool ROW_FAST, class Body>
+cudaError_t launch_one_tm2(const Body &body, const CUtensorMap &tm0, const CUtensorMap &tm1, int nrows,
+                           cudaStream_t s) {
+    auto kern = k_pass_tm2<N, ROW_FAST, Body>;
+    constexpr size_t smem = Body::template smem<N, ROW_FAST>();
+    static_assert(smem <= kSmemMax, "pass needs more shared memory than a CTA has");
+    if constexpr (smem > 48 * 1024) {
+        static unsigned long long done_mask = 0;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const unsigned long long bit = 1ull << (dev & 63);
+        if (!(__atomic_load_n(&done_mask, __ATOMIC_ACQUIRE) & bit)) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            __atomic_fetch_or(&done_mask, bit, __ATOMIC_ACQ_REL);
+        }
+    }
+    using S = Shape<N, Body::EPT, Body::TT>;
+    const int gx = (nrows + S::ROWS - 1) / S::ROWS;
+    if (gx == 0) return cudaSuccess;
+    kern<<<gx, S::THREADS, smem, s>>>(body, tm0, tm1);
+    return cudaGetLastError();
+}
+
 // Launch of a pass that exists only for the lengths where Body::staged<N>() holds.
 template <bool ROW_FAST, class Body>
 cudaError_t launch_staged_len(int n, const Body &body, int nrows, cudaStream_t s) {
@@ -207,6 +232,12 @@ cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_COMPLEX> &b, cudaStream_t 
 cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_SQRT_REAL> &b, cudaStream_t s);
 cudaError_t launch_fwd_rows(int n, const FwdRowsT<FWD_PADDED> &b, cudaStream_t s);
 cudaError_t launch_spectrum(int n, const SpectrumCols &b, cudaStream_t s);
+// The spectrum pass with staged transfers (lengths 512 .. 2048; spectrum_staged_rows
+// gives the rows per CTA, 0 elsewhere); tm_hf, tm_hdz: the centred transfers
+// as [n_slow][n_fast] 8-byte elements, boxes of rows x 256.
+int spectrum_staged_rows(int n);
+cudaError_t launch_spectrum_staged(int n, const SpectrumColsT &b, const CUtensorMap &tm_hf, const CUtensorMap &tm_hdz,
+                                   cudaStream_t s);
 cudaError_t launch_recon_a(int n, const ReconA &b, int nbatch, cudaStream_t s);
 // Pass A with the tensor-map transposed store (lengths where recon_a_tstore holds;
 // tm: T as [nbatch][ny_out = n][nx] 8-byte elements, boxes of 4 x 256 x 1).

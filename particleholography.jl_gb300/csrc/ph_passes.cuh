@@ -155,6 +155,17 @@ __global__ void __launch_bounds__(Shape<N, Body::EPT, Body::TT>::THREADS, min_bl
     body.template run<N, ROW_FAST>(ph_smem, r, j, &tm);
 }
 
+// A pass whose body takes two tensor maps.
+template <int N, bool ROW_FAST, class Body>
+__global__ void __launch_bounds__(Shape<N, Body::EPT, Body::TT>::THREADS, min_blocks<N, Body>())
+    k_pass_tm2(const Body body, const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1) {
+    extern __shared__ __align__(128) unsigned char ph_smem[];
+    const int t = threadIdx.x;
+    const int r = ThreadMap<N, Body::EPT, Body::TT, ROW_FAST>::row(t);
+    const int j = ThreadMap<N, Body::EPT, Body::TT, ROW_FAST>::j(t);
+    body.template run<N, ROW_FAST>(ph_smem, r, j, &tm0, &tm1);
+}
+
 __device__ __forceinline__ int shift_idx(int i, int n) {   // centred index of natural frequency i
     int s = i + (n >> 1);
     return s >= n ? s - n : s;
@@ -331,6 +342,70 @@ struct SpectrumCols : PassBase {
                 const size_t c = (size_t)shift_idx(ky, N) * nx + sx;
                 const float2 x0 = cscale(cmul(v, hf[c]), lpf != nullptr ? scale * lpf[c] : scale);
                 const float2 d = hdz[c];
+                state[(size_t)kx * N + ky] =
+                    make_float4(x0.x, x0.y, __uint_as_float(phase_turns_u32(d, ptab)), log2_modulus(d));
+            });
+    }
+};
+
+// The spectrum pass with the transfers staged: the columns of the front and
+// slice transfers that the CTA's ROWS rows kx need are loaded into shared
+// memory as [ky][kx mod ROWS] by tensor-map boxes of ROWS x 256 (issued before
+// the transform, so they overlap it; kx's centred column is one of ROWS
+// consecutive ones, ky's centred row range of a box is contiguous because N/2
+// is a multiple of 256).  The outputs then read them conflict-free instead of
+// gathering ROWS-element pieces from ROWS different lines per warp load.  One
+// item, no low-pass mask, N a multiple of 512 (so that N/2 is one of 256),
+// nx a multiple of 2 ROWS.
+struct SpectrumColsT : SpectrumCols {
+    int *err;   // raised if the staging wait times out
+    template <int N, bool RF>
+    static constexpr size_t xbytes() { return round128(Shape<N, EPT, TT>::template smem_bytes<RF>()); }
+    template <int N>
+    static constexpr size_t tbytes() { return (size_t)N * Shape<N, EPT, TT>::ROWS * 8; }   // one staged transfer
+    template <int N, bool RF>
+    static constexpr size_t smem() { return xbytes<N, RF>() + 2 * tbytes<N>() + 16; }
+    template <int N>
+    static constexpr bool staged() {
+        return N % 512 == 0 && Shape<N, EPT, TT>::ROWS >= 4 && Shape<N, EPT, TT>::ROWS <= 32 &&
+               smem<N, true>() <= kSmemMax;
+    }
+    template <int N, bool RF>
+    __device__ __forceinline__ void run(unsigned char *smem, int r, int j, const void *tm_hf,
+                                        const void *tm_hdz) const {
+        using S = Shape<N, EPT, TT>;
+        constexpr int ROWS = S::ROWS;
+        float2 *shf = reinterpret_cast<float2 *>(smem + xbytes<N, RF>());
+        float2 *shdz = shf + (size_t)N * ROWS;
+        uint64_t *bar = reinterpret_cast<uint64_t *>(smem + xbytes<N, RF>() + 2 * tbytes<N>());
+        const int kx0 = blockIdx.x * ROWS;
+        const int kx = kx0 + r;
+        const bool valid = kx < nx;
+        const int sx0 = shift_idx(kx0, nx);   // the centred columns of kx0 .. kx0 + ROWS - 1
+        if (threadIdx.x == 0) {
+            mbar_init(bar, 1);
+            mbar_fence_init();
+            mbar_arrive_expect_tx(bar, (uint32_t)(2 * tbytes<N>()));
+#pragma unroll 1
+            for (int q = 0; q < N / 256; ++q) {
+                const int sy = shift_idx(q * 256, N);
+                tma_load_2d(shf + (size_t)q * 256 * ROWS, tm_hf, sx0, sy, bar);
+                tma_load_2d(shdz + (size_t)q * 256 * ROWS, tm_hdz, sx0, sy, bar);
+            }
+        }
+        __syncthreads();   // the barrier is initialised before any thread waits on it
+        bool ready = false;
+        fft_row<N, S::E, false>(
+            xrow<N, EPT, TT, RF>(smem, r), j, tw,
+            [&](int, int y) -> float2 { return valid ? a1[(size_t)kx * N + y] : make_float2(0.f, 0.f); },
+            [&](int, int ky, float2 v) {
+                if (!ready) {   // (the first output: the boxes have landed)
+                    mbar_wait(bar, 0, err);
+                    ready = true;
+                }
+                if (!valid) return;
+                const float2 x0 = cscale(cmul(v, shf[ky * ROWS + r]), scale);
+                const float2 d = shdz[ky * ROWS + r];
                 state[(size_t)kx * N + ky] =
                     make_float4(x0.x, x0.y, __uint_as_float(phase_turns_u32(d, ptab)), log2_modulus(d));
             });

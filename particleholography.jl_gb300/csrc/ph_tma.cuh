@@ -158,6 +158,18 @@ __device__ __forceinline__ void tma_store_3d(const void *tmap, const void *src, 
                  "r"(smem_addr(src)), "r"(x), "r"(y), "r"(z)
                  : "memory");
 }
+// ---- tiled bulk loads (global -> shared through a tensor map)
+
+// One box of a 2-D tensor map at element coordinates (x, y) into shared
+// memory (128-byte aligned); completion counts the box's bytes on `bar`.
+__device__ __forceinline__ void tma_load_2d(void *dst, const void *tmap, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_addr(dst)),
+        "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(bar))
+        : "memory");
+}
+
 // The 4-D form: element coordinates (x, y, z, w).
 __device__ __forceinline__ void tma_store_4d(const void *tmap, const void *src, int x, int y, int z, int w) {
     asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(tmap),
