@@ -1009,7 +1009,8 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
     for (int k0 = first; k0 < first + slices; k0 += L.batch) {
         const int nb = std::min(L.batch, first + slices - k0);
         const ph_tuning *tu = tuning_of(ctx, nx, ny);
-        const int group = recon_group(nb, row_blocks_a, recon_a_chain(ny), tu ? tu->group_cap : 0);
+        const bool ts_shape = recon_a_tstore(ny) && y0 == 0 && ny_out == ny;   // the tensor-map store form
+        const int group = recon_group(nb, row_blocks_a, recon_a_chain(ny, ts_shape), tu ? tu->group_cap : 0);
         const auto fill_a = [&](auto &a) {
             a.state = state;
             a.t = t;
@@ -1023,7 +1024,7 @@ int issue_recon_slices(ph_ctx *ctx, ReconKind kind, float *proj, int32_t *argmin
             a.err = static_cast<int *>(ctx->small);
         };
         CUtensorMap tm;
-        if (recon_a_tstore(ny) && y0 == 0 && ny_out == ny && t_store_map(&tm, t, nx, ny_out, nb, recon_a_tstore_box(ny))) {
+        if (ts_shape && t_store_map(&tm, t, nx, ny_out, nb, recon_a_tstore_box(ny))) {
             ReconATStore a{};
             fill_a(a);
             PH_TRY(pass(ctx, s, "recon_a", [&] { return launch_recon_a_tstore(ny, a, tm, nb, s); }));

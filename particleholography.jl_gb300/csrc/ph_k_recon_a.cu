@@ -12,7 +12,14 @@ int recon_a_rows(int n) {
     return 1;
 }
 
-bool recon_a_chain(int n) {
+bool recon_a_chain(int n, bool tstore) {
+    if (tstore) {
+        switch (n) {
+#define PH_CHAIN_AT(N) case N: return ReconATStore::form<N, true>() == ReconATStore::FORM_CHAIN;
+            PH_CHAIN_AT(256) PH_CHAIN_AT(512) PH_CHAIN_AT(1024) PH_CHAIN_AT(2048) PH_CHAIN_AT(4096)
+#undef PH_CHAIN_AT
+        }
+    }
     switch (n) {
 #define PH_CHAIN_A(N) case N: return ReconA::form<N, true>() == ReconA::FORM_CHAIN;
         PH_FOR_EACH_N(PH_CHAIN_A)

@@ -259,7 +259,8 @@ cudaError_t launch_gs_col_ts(int n, const GsColT &b, const CUtensorMap &tm, cuda
 cudaError_t launch_gs_row_ts(int n, const GsRowMidT &b, const CUtensorMap &tm, cudaStream_t s);
 cudaError_t launch_recon_b_group(int n, const ReconB<EPI_PROJ, true> &b, cudaStream_t s);
 int recon_a_rows(int n);   // rows per pass A CTA for transform length n
-bool recon_a_chain(int n); // whether pass A at length n advances X by the product chain
+bool recon_a_chain(int n, bool tstore = false);   // whether pass A at length n (in the tensor-map
+                                                  // store form) advances X by the product chain
 cudaError_t launch_recon_b(int n, const ReconB<EPI_PROJ> &b, cudaStream_t s);
 cudaError_t launch_recon_b(int n, const ReconB<EPI_VOL> &b, cudaStream_t s);
 cudaError_t launch_recon_b(int n, const ReconB<EPI_CVOL> &b, cudaStream_t s);

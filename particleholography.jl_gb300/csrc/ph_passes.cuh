@@ -462,14 +462,15 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
     // The chain saves the per-voxel sin/cos; the direct forms move fewer
     // shared-memory bytes per voxel and need fewer registers.  Measured per
     // pass A launch, chain against the staged state: 2048 3.7 % and 512 2.7 %
-    // faster; 1024 18 % slower (register spills); 4096 6 % slower (its cluster
-    // store competes for shared-memory bandwidth); 256 22 % slower (slice groups
+    // faster; 4096 with the tensor-map store 1.5 % faster; 1024 18 % slower
+    // (register spills); 4096 with the pull store 6 % slower (its distributed
+    // loads compete for shared-memory bandwidth); 256 22 % slower (slice groups
     // of 6 slices do not repay the chain's start).  Other lengths keep the
     // direct form.
     enum { FORM_NONE = 0, FORM_X0 = 1, FORM_STATE = 2, FORM_CHAIN = 3 };
     template <int N>
     static constexpr bool chain() {
-        return PH_RECONA_CHAIN >= 0 ? PH_RECONA_CHAIN != 0 : (N == 2048 || N == 512);
+        return PH_RECONA_CHAIN >= 0 ? PH_RECONA_CHAIN != 0 : (N == 2048 || N == 512 || (TSTORE && N == 4096));
     }
     template <int N, bool RF>
     static constexpr int rec_stride() {   // float2 between rows: conflict-free for the load pattern
