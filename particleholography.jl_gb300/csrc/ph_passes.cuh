@@ -463,7 +463,7 @@ struct ReconAT : PassBase, std::conditional_t<GROUPED, ReconItems, NoItems> {
     // shared-memory bytes per voxel and need fewer registers.  Measured per
     // pass A launch, chain against the staged state: 2048 3.7 % and 512 2.7 %
     // faster; 4096 with the tensor-map store 1.5 % faster; 1024 18 % slower
-    // (register spills); 4096 with the pull store 6 % slower (its distributed
+    // (register spills; 6 % slower in the tensor-map store form, unspilled); 4096 with the pull store 6 % slower (its distributed
     // loads compete for shared-memory bandwidth); 256 22 % slower (slice groups
     // of 6 slices do not repay the chain's start).  Other lengths keep the
     // direct form.
