@@ -151,7 +151,11 @@ def test_gs_tiny_field(ph, cuda, n):
     assert rel_l2(to_np(u.data), ref.phase_retrieval_holo(h1, h2, tp, tpi, 3, n)) < REL_L2
 
 
-@pytest.mark.parametrize("n_fast,n_slow", [(2048, 1024), (1024, 2048)])
+# (2048, 768) / (768, 2048): the 4-row passes at 2048 walk 192 blocks, a second
+# round on 40 CTAs; (2048, 6) / (2048, 3): fewer blocks than CTAs, the one
+# block of the row pass partial.
+@pytest.mark.parametrize("n_fast,n_slow", [(2048, 1024), (1024, 2048), (2048, 768), (768, 2048), (2048, 6),
+                                           (2048, 3)])
 def test_gs_rectangular_through_abi(ph, cuda, n_fast, n_slow):
     """Rectangular frames through the C ABI (the Python mirror keeps the
     reference's square assertion): the staged column and row passes run at
