@@ -63,6 +63,20 @@ def test_chain_length_shards(ph, cuda):
     assert rel_l2(p, p_ref) < REL_L2 and np.mean(a == a_ref) >= ARGMIN_AGREE
 
 
+def test_chain_length_shards_4096(ph, cuda):
+    """At 4096 pass A's tensor-map store form (full frames) also runs the
+    product chain: shards (chains of 10 and 14 slices) agree with the single
+    call (one chain of 24) to the chain's rounding."""
+    from ph_gb300 import parallel
+    n, slices, cut = 4096, 24, 10
+    wf, tf, td = _tensors(ph, cuda, *_case(n, seed=7, slices_dz=-100.0))
+    p1, a1 = (to_np(t) for t in ph.cu_get_reconst_xyprojection(wf, tf, td, slices, return_argmin=True))
+    packed = parallel.reconst_xyprojection_range(wf, tf, td, 0, cut)
+    parallel.reconst_xyprojection_range(wf, tf, td, cut, slices, packed=packed, accumulate=True)
+    p, a = (to_np(t) for t in parallel.unpack_projection(packed))
+    assert rel_l2(p, p1) < 1e-5 and np.mean(a == a1) >= ARGMIN_AGREE
+
+
 def test_empty_shard_is_identity(ph, cuda):
     from ph_gb300 import parallel, _lib
     wf, tf, td = _tensors(ph, cuda, *_case(64, seed=3))
